@@ -1,0 +1,377 @@
+"""Benchmark: CPAB transform_data forward + backward (dtheta and d(data)).
+
+Workload (the configuration the headline metric is quoted on): 2D
+tessellation [3,3] with zero boundary (d = 34), 64 theta ~ N(0, 0.5^2 I), data
+[64, 3, 224, 224] uniform[0,1] smoothed by a 5x5 box filter, transform_data on
+a 224x224 grid, loss = MSE against the same images warped by a second theta.
+One step = forward + backward of that loss over the whole batch
+(64 * 224 * 224 = 3,211,264 point trajectories of 50 steps).  Metric: points/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl {gb300,reference}]
+
+Under torchrun (N > 1) every rank runs the full batch with its own seeds
+(weak scaling, no data-path collective); the slowest rank's time sets the
+aggregate.  --impl reference times the reference's CPU implementation of the
+same step (the C oracle port, all host threads) on a bounded sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+import torch
+import torch.nn.functional as F
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = 'points/s fwd+dθ bwd, 2D 3×3 224² b64: fused vs plain GPU, err≤1e-5 vs FP64'
+NC = [3, 3]
+BATCH, SIZE, CHANNELS, NSTEPS = 64, 224, 3, 50
+THETA_STD = 0.5
+L2_BYTES = 129 * 2 ** 20
+# algorithmic work per point trajectory (2D, 50 steps): forward 17 flop/step,
+# adjoint 37 flop/step; interpolation 8*C bytes (forward), 12*C (backward)
+FLOP_FWD_STEP, FLOP_ADJ_STEP = 17, 37
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--cpu-sample-images', type=int, default=1)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+def make_inputs(T, device, seed_offset=0):
+    d = T.get_theta_dim()
+    g0 = torch.Generator().manual_seed(0 + seed_offset)
+    g1 = torch.Generator().manual_seed(1 + seed_offset)
+    g2 = torch.Generator().manual_seed(2 + seed_offset)
+    theta = THETA_STD * torch.randn(BATCH, d, generator=g0)
+    raw = torch.rand(BATCH, CHANNELS, SIZE, SIZE, generator=g1)
+    data = F.avg_pool2d(raw, kernel_size=5, stride=1, padding=2, count_include_pad=False)
+    theta2 = THETA_STD * torch.randn(BATCH, d, generator=g2)
+    with torch.no_grad():
+        target = T.transform_data(data.to(device), theta2.to(device), [SIZE, SIZE])
+    return theta, data.contiguous(), target.cpu().contiguous()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples while the timed region runs."""
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.FIELDS,
+                 '--format=csv,noheader,nounits', '-lms', '100'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(',')]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(smax),
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def reduce_max(values, device):
+    """Element-wise max over ranks (the slowest rank sets the job time)."""
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def time_events(fn, steps, flush=None, stream=None):
+    """Per-iteration CUDA-event times (ms) on the launching stream; L2 flushed
+    before each iteration outside the timed window."""
+    stream = stream or torch.cuda.current_stream()
+    times = []
+    for _ in range(steps):
+        if flush is not None:
+            flush()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return times
+
+
+def run_gb300(args):
+    from libcpab_gb300 import Cpab, _native as N
+    from libcpab_gb300.functions import basis_on
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+    device = torch.device('cuda', local)
+    torch.cuda.set_device(device)
+    T = Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True)
+    theta_h, data_h, target_h = make_inputs(T, device, seed_offset=10 * rank)
+    theta_h, data_h, target_h = theta_h.pin_memory(), data_h.pin_memory(), target_h.pin_memory()
+    theta = theta_h.to(device)
+    data = data_h.to(device)
+    target = target_h.to(device)
+    flush_buf = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=device)
+    flush = lambda: flush_buf.fill_(1.0)
+
+    def step():
+        th = theta.detach().requires_grad_(True)
+        dd = data.detach().requires_grad_(True)
+        out = T.transform_data(dd, th, [SIZE, SIZE])
+        loss = F.mse_loss(out, target)
+        loss.backward()
+        return loss, th.grad, dd.grad
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    clocks = ClockSampler(local) if rank == 0 else None
+    if clocks:
+        clocks.start()
+    times = time_events(step, args.steps, flush)
+    barrier()
+    ms_step = sum(times) / len(times)
+
+    # e2e through the public API with host buffers: H2D inputs, D2H loss + dtheta
+    def step_e2e():
+        th = theta_h.to(device, non_blocking=True).requires_grad_(True)
+        dd = data_h.to(device, non_blocking=True).requires_grad_(True)
+        tg = target_h.to(device, non_blocking=True)
+        out = T.transform_data(dd, th, [SIZE, SIZE])
+        loss = F.mse_loss(out, tg)
+        loss.backward()
+        res = torch.cat([loss.detach().reshape(1), th.grad.reshape(-1)]).to('cpu',
+                                                                          non_blocking=True)
+        return res
+    for _ in range(2):
+        step_e2e()
+    torch.cuda.synchronize()
+    e2e_times = time_events(step_e2e, args.steps, flush)
+    barrier()
+    ms_e2e = sum(e2e_times) / len(e2e_times)
+    h2d = (theta_h.numel() + data_h.numel() + target_h.numel()) * 4
+    d2h = (1 + theta_h.numel()) * 4
+
+    # per-kernel timing of the two hot launches (same inputs), for the roofline
+    params = T.params
+    basis = basis_on(params, device)
+    A, _, E = N.cell_tables(NC, NSTEPS, theta, basis)
+    lin = torch.cat([torch.linspace(0, 1, SIZE, device=device)] * 2).contiguous()
+    out, grid = N.transform_data(NC, NSTEPS, lin, [SIZE, SIZE], E, data, save_grid=True)
+    gout = (2.0 / out.numel()) * (out - target)
+    ws_need = N.load().cpab_transform_data_backward_workspace(2, N._ints(NC), NSTEPS, 0,
+                                                               N._ints([SIZE, SIZE]), BATCH)
+    ws = torch.empty(ws_need, dtype=torch.uint8, device=device)
+    t_fwd = time_events(lambda: N.transform_data(NC, NSTEPS, lin, [SIZE, SIZE], E, data,
+                                                 save_grid=True), args.steps, flush)
+    t_bwd = time_events(lambda: N.transform_data_backward(NC, NSTEPS, 0, lin, [SIZE, SIZE], A, E,
+                                                          grid, data, basis, gout,
+                                                          workspace=ws), args.steps, flush)
+    clk = clocks.stop() if clocks else None
+    status = N.device_status()
+
+    ms_max, ms_e2e_max = reduce_max([ms_step, ms_e2e], device)
+    pts = BATCH * SIZE * SIZE
+    value = world * pts / (ms_max / 1e3)
+    e2e_value = world * pts / (ms_e2e_max / 1e3)
+
+    bwd_ms = sum(t_bwd) / len(t_bwd)
+    fwd_ms = sum(t_fwd) / len(t_fwd)
+    bwd_flop = pts * NSTEPS * (FLOP_FWD_STEP + FLOP_ADJ_STEP)
+    sm_mhz = clk['sm_mhz'] if clk else 2070.0
+    fp32_peak = 152 * 128 * 2 * 2070e6 / 1e12        # TFLOP/s at the maximum SM clock
+    achieved = bwd_flop / (bwd_ms / 1e3) / 1e12
+    fwd_bytes = pts * 8 * CHANNELS
+    result = None
+    if rank == 0:
+        result = {
+            'metric': METRIC, 'value': value, 'unit': 'points/s', 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_max,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': 'transform_data 2D tess [3,3] zero_boundary, 64 theta ~ '
+                                   'N(0,0.25I), data [64,3,224,224] box-filtered U[0,1], '
+                                   'MSE vs second warp, fwd + dtheta/d(data) bwd',
+                       'tess_size': NC, 'batch': BATCH, 'outsize': [SIZE, SIZE],
+                       'nstepsolver': NSTEPS, 'gradient': params.gradient,
+                       'l2': 'flushed before every timed iteration (%d MB write)'
+                             % (2 * L2_BYTES // 2 ** 20),
+                       'parallelism': 'dp%d' % world},
+            'e2e': {'value': e2e_value, 'unit': 'points/s', 'h2d_bytes_per_step': h2d,
+                    'd2h_bytes_per_step': d2h, 'ms_per_step': ms_e2e_max},
+            'gpu_launches': 4 * args.steps,
+            'roofline': {'bound': 'fp32', 'kernel': 'k_transform_data_backward (+finalize)',
+                         'achieved': achieved, 'peak': fp32_peak, 'unit': 'TFLOP/s',
+                         'frac': achieved / fp32_peak,
+                         'peak_source': 'derived: 152 SM x 128 FP32 lanes x 2 flop x 2070 MHz '
+                                        '(MEASURED_PEAKS has HBM and bf16 only)',
+                         'flop_per_launch': bwd_flop, 'ms_per_launch': bwd_ms,
+                         'traffic': None},
+            'forward_kernel': {'name': 'k_transform_data', 'ms_per_launch': fwd_ms,
+                               'flop_per_launch': pts * NSTEPS * FLOP_FWD_STEP,
+                               'tflops': pts * NSTEPS * FLOP_FWD_STEP / (fwd_ms / 1e3) / 1e12,
+                               'interp_gbs': fwd_bytes / (fwd_ms / 1e3) / 1e9},
+            'clocks': clk, 'device_status': status,
+        }
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return result
+
+
+def cpu_reference_step(sample, orc, T_h, nc):
+    """The reference's CPU implementation of one step on a sample of images:
+    forward op + interpolation, interpolation backward, analytic-gradient
+    backward op (oracle/cpab_oracle.c restates libcpab/core/cpab_ops.cpp and
+    libcpab/pytorch/interpolation.py)."""
+    theta, data, target, grid, As, Bs = sample
+    out_grid = orc.forward(nc, NSTEPS, grid, T_h)
+    out = orc.interpolate(data, out_grid, [SIZE, SIZE])
+    gout = (2.0 * (out - target) / out.size).astype(np.float32)
+    ddata, dgrid = orc.interpolate_backward(data, out_grid, [SIZE, SIZE], gout)
+    dtheta = orc.backward(nc, NSTEPS, grid, As, Bs, dgrid)
+    return dtheta, ddata
+
+
+def cpu_sample(T, n_img):
+    from oracle.oracle import step_maps_fp64
+    theta, data, target = make_inputs_cpu(T)
+    th = theta[:n_img].numpy()
+    basis = T.params.basis
+    Tm = step_maps_fp64(basis, th, 2, NSTEPS)[:, :, :2, :].astype(np.float32)
+    As = (basis @ th.astype(np.float64).T).T.reshape(n_img, -1, 2, 3).astype(np.float32)
+    Bs = basis.T.reshape(basis.shape[1], -1, 2, 3).astype(np.float32)
+    lin = np.linspace(0, 1, SIZE, dtype=np.float32)
+    gx, gy = np.meshgrid(lin, lin, indexing='xy')
+    grid = np.stack([gx.reshape(-1), gy.reshape(-1)]).astype(np.float32)
+    return (th, data[:n_img].numpy(), target[:n_img].numpy(), grid, As, Bs), Tm
+
+
+def make_inputs_cpu(T):
+    d = T.get_theta_dim()
+    theta = THETA_STD * torch.randn(BATCH, d, generator=torch.Generator().manual_seed(0))
+    raw = torch.rand(BATCH, CHANNELS, SIZE, SIZE, generator=torch.Generator().manual_seed(1))
+    data = F.avg_pool2d(raw, kernel_size=5, stride=1, padding=2, count_include_pad=False)
+    # the target only enters the loss value; a smoothed copy keeps the sample self-contained
+    target = F.avg_pool2d(data, kernel_size=3, stride=1, padding=1, count_include_pad=False)
+    return theta, data.contiguous(), target.contiguous()
+
+
+def run_cpu_baseline(steps, n_img):
+    """Time the reference CPU path on n_img images; returns points/s and info."""
+    from oracle.oracle import Oracle
+    from libcpab_gb300.tessellation import make_tessellation
+    orc = Oracle()
+    threads = orc.num_threads()
+
+    class _T:
+        pass
+    T = _T()
+    tess = make_tessellation(NC, True, False)
+    T.params = _T()
+    T.params.basis = tess.B
+    T.get_theta_dim = lambda: tess.B.shape[1]
+    sample, Tm = cpu_sample(T, n_img)
+    times = []
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        cpu_reference_step(sample, orc, Tm, NC)
+        times.append(time.perf_counter() - t0)
+    pts = n_img * SIZE * SIZE
+    return pts / statistics.median(times), threads, \
+        '%d of 64 images (%d points) per step, median of %d' % (n_img, pts, len(times))
+
+
+def main():
+    args = parse()
+    rank, world, _ = dist_env()
+    if args.impl == 'reference':
+        if rank != 0:
+            return
+        v, cores, sample = run_cpu_baseline(max(1, args.steps // 4), args.cpu_sample_images)
+        line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'points/s',
+                'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+                'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+                'dtype': 'f32', 'data': 'synthetic',
+                'config': {'workload': 'transform_data 2D tess [3,3], 224x224, MSE fwd + '
+                                       'reference analytic dtheta + d(data) backward',
+                           'parallelism': 'cpu'},
+                'cpu_baseline': {'value': v, 'unit': 'points/s', 'cores': cores,
+                                 'kind': 'port', 'sample': sample},
+                'e2e': {'value': v, 'unit': 'points/s', 'h2d_bytes_per_step': 0,
+                        'd2h_bytes_per_step': 0}}
+        print(json.dumps(line))
+        return
+    res = run_gb300(args)
+    if rank == 0 and res is not None:
+        if world == 1:
+            v, cores, sample = run_cpu_baseline(1, args.cpu_sample_images)
+            res['cpu_baseline'] = {'value': v, 'unit': 'points/s', 'cores': cores,
+                                   'kind': 'port', 'sample': sample}
+        print(json.dumps(res))
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,187 @@
+/*
+ * cpab_gb300.h -- C ABI of the GB300 (sm_103a) CPAB integration library.
+ *
+ * Plain pointers and sizes only.  Every pointer argument named like a tensor
+ * is a CUDA device pointer to contiguous float32 (or int32) memory on the
+ * current device; `nc`, `size` and `outsize` are host arrays of `ndim` ints.
+ * `stream` is a cudaStream_t (NULL = legacy default stream).  Work is only
+ * enqueued: no entry point synchronises the host except cpab_device_status.
+ *
+ * Every entry point returns CPAB_OK (0) or an error code; the message for
+ * the last error of the calling thread is returned by cpab_last_error().
+ * Nothing here terminates the process (the reference calls exit() on a CUDA
+ * error: libcpab/pytorch/transformer_cuda.cu:8-16).
+ *
+ * Tensor layouts are the reference's (libcpab/pytorch/transformer_cuda.cpp:
+ * 17-70, libcpab/pytorch/interpolation.py):
+ *   points  [ndim, nP] (shared by all theta, broadcast=0) or
+ *           [n_theta, ndim, nP] (one grid per theta, broadcast=1)
+ *   tables  [n_theta, nC, ndim, ndim+1]  (A, T or E; row-major affine maps)
+ *   basis   [D, d] with D = nC * ndim * (ndim+1), float32
+ *   theta   [n_theta, d]
+ *   data    [nb, C, size[0] (, size[1] (, size[2]))]
+ *   images  [nb, C, outsize[0] (, outsize[1] (, outsize[2]))]
+ * nC = nc[0] (1D), 4*nc[0]*nc[1] (2D), 5*nc[0]*nc[1]*nc[2] (3D).
+ */
+#ifndef CPAB_GB300_H
+#define CPAB_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define CPAB_API __attribute__((visibility("default")))
+#else
+#define CPAB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CPAB_OK 0
+#define CPAB_ERR_ARGUMENT 1     /* invalid size, pointer or option        */
+#define CPAB_ERR_CUDA 2         /* a CUDA runtime call or launch failed   */
+#define CPAB_ERR_UNSUPPORTED 3  /* configuration beyond a kernel's limits */
+#define CPAB_ERR_WORKSPACE 4    /* workspace missing or too small         */
+
+/* Gradient modes of cpab_backward / cpab_transform_data_backward. */
+#define CPAB_GRAD_REFERENCE 0   /* the reference's midpoint-rule analytic gradient */
+#define CPAB_GRAD_EXACT 1       /* exact derivative of the forward map             */
+
+/* Bits reported by cpab_device_status. */
+#define CPAB_DEV_TMA_TIMEOUT 1u /* a bulk copy to shared memory did not complete */
+#define CPAB_DEV_BAD_CELL 2u    /* a cell index fell outside [0, nC)             */
+
+/* Message of the calling thread's last error ("" if none). */
+CPAB_API const char *cpab_last_error(void);
+
+/* ABI version (major*10000 + minor*100 + patch). */
+CPAB_API int cpab_version(void);
+
+/*
+ * Number of cells for a tessellation (nC), or -1 for invalid arguments.
+ */
+CPAB_API int cpab_num_cells(int ndim, const int *nc);
+
+/*
+ * Per-(theta, cell) tables from theta: A = B theta (reshaped), and the step
+ * maps T = expm(dT [A;0]) (top ndim rows) and E = T - I, dT = 1/nsteps.
+ * Any of A, T, E may be NULL.  E is computed in compensated form (no I + small
+ * cancellation).
+ * Replaces libcpab/pytorch/transformer.py:146-155 (B copied host->device per
+ * call, As = B theta^T, expm of libcpab/pytorch/expm.py with its host sync).
+ */
+CPAB_API int cpab_cell_tables(int ndim, const int *nc, int nsteps, const float *theta, int n_theta,
+                     int d, const float *basis, float *A, float *T, float *E, void *stream);
+
+/*
+ * Forward integration with the reference's own step maps:
+ * nsteps times { c = cell(p); p = T_c [p;1] }.  out is [n_theta, ndim, nP].
+ * Drop-in for cpab_gpu.forward(points, trels, nstepsolver, nc)
+ * (libcpab/pytorch/transformer_cuda.cpp:17-41, kernels
+ * libcpab/core/cpab_ops.cu:268-388).
+ */
+CPAB_API int cpab_forward(int ndim, const int *nc, int nsteps, const float *points, int broadcast,
+                 long long nP, const float *trels, int n_theta, float *out, void *stream);
+
+/*
+ * Forward integration with compensated increments: p = p + E_c [p;1].
+ * The arithmetic used by Cpab.transform_grid.  ties (device counter, may be
+ * NULL) is incremented once per cell lookup resolved by the FP64 path.
+ */
+CPAB_API int cpab_integrate(int ndim, const int *nc, int nsteps, const float *points, int broadcast,
+                   long long nP, const float *E, int n_theta, float *out,
+                   unsigned long long *ties, void *stream);
+
+/*
+ * Workspace bytes needed by cpab_backward for this problem on the current
+ * device (0 on invalid arguments; see cpab_last_error).
+ */
+CPAB_API size_t cpab_backward_workspace(int ndim, const int *nc, int nsteps, long long nP, int n_theta);
+
+/*
+ * dL/dtheta [n_theta, d] (and optionally dL/dpoints [n_theta, ndim, nP]) from
+ * grad_out = dL/d(out) [n_theta, ndim, nP].
+ *   mode CPAB_GRAD_REFERENCE: the reference's analytic gradient (midpoint-rule
+ *     sensitivity, libcpab/core/cpab_ops.cu:390-697) computed in reverse mode;
+ *     needs A.
+ *   mode CPAB_GRAD_EXACT: exact adjoint of cpab_integrate; needs A and E.
+ * Replaces cpab_gpu.backward (libcpab/pytorch/transformer_cuda.cpp:43-70) and
+ * the contraction gradient.mul_(grad).sum(dim=(2,3))
+ * (libcpab/pytorch/transformer.py:186-202), without the [d, n_theta, ndim, nP]
+ * intermediate.  The result is deterministic (no floating-point atomics).
+ */
+CPAB_API int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *points,
+                  int broadcast, long long nP, const float *A, const float *E, int n_theta,
+                  const float *basis, int d, const float *grad_out, float *dtheta,
+                  float *dpoints, void *workspace, size_t workspace_bytes,
+                  unsigned long long *ties, void *stream);
+
+/*
+ * Linear / bilinear / trilinear sampling with clamp-to-edge.  grid is
+ * [nb, ndim, prod(outsize)] with the meshgrid's x fastest; out is the image
+ * layout above.  Replaces libcpab/pytorch/interpolation.py:12-172.
+ */
+CPAB_API int cpab_interpolate(int ndim, const float *data, int nb, int C, const int *size,
+                     const float *grid, const int *outsize, float *out, void *stream);
+
+/*
+ * Backward of cpab_interpolate: ddata (overwritten, may be NULL) and dgrid
+ * (overwritten, may be NULL) from grad_out (image layout).  ddata is a
+ * scatter-add with float atomics, like the reference's autograd.
+ */
+CPAB_API int cpab_interpolate_backward(int ndim, const float *data, int nb, int C, const int *size,
+                              const float *grid, const int *outsize, const float *grad_out,
+                              float *ddata, float *dgrid, void *stream);
+
+/*
+ * Fused transform_data forward: meshgrid -> cpab_integrate -> interpolate in
+ * one kernel.  lin holds the meshgrid's per-axis coordinates, concatenated
+ * (outsize[0] + ... + outsize[ndim-1] floats, e.g. torch.linspace(0,1,n)).
+ * E is [nb, nC, ndim, ndim+1].  grid_out (may be NULL) receives the
+ * transformed points as [nb, ndim, prod(outsize)] in image order (last axis
+ * fastest), for cpab_transform_data_backward in reference mode.
+ * Replaces libcpab/cpab.py:304-331 (uniform_meshgrid, transform_grid,
+ * interpolate as separate passes).
+ */
+CPAB_API int cpab_transform_data(int ndim, const int *nc, int nsteps, const float *lin,
+                        const int *outsize, const float *E, int nb, const float *data, int C,
+                        const int *size, float *out, float *grid_out,
+                        unsigned long long *ties, void *stream);
+
+CPAB_API size_t cpab_transform_data_backward_workspace(int ndim, const int *nc, int nsteps, int mode,
+                                              const int *outsize, int nb);
+
+/*
+ * Fused transform_data backward from grad_out = dL/d(out) (image layout):
+ * ddata (overwritten, may be NULL) and dtheta [nb, d].  Mode
+ * CPAB_GRAD_REFERENCE needs A and grid_saved (from cpab_transform_data);
+ * CPAB_GRAD_EXACT needs A and E.
+ */
+CPAB_API int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, int mode,
+                                 const float *lin, const int *outsize, const float *A,
+                                 const float *E, const float *grid_saved, int nb,
+                                 const float *data, int C, const int *size, const float *basis,
+                                 int d, const float *grad_out, float *ddata, float *dtheta,
+                                 void *workspace, size_t workspace_bytes,
+                                 unsigned long long *ties, void *stream);
+
+/*
+ * Cell index of every point ([ndim, nP] -> int32 [nP]), bit-identical to the
+ * reference's C++/CUDA lookup (libcpab/core/cpab_ops.cpp:26-190).
+ */
+CPAB_API int cpab_findcellidx(int ndim, const int *nc, const float *points, long long nP, int *out,
+                     unsigned long long *ties, void *stream);
+
+/*
+ * Synchronise the current device and report the device error word (the
+ * CPAB_DEV_* bits raised by kernels since the last clear).  clear != 0 resets
+ * it.  Returns CPAB_OK, or CPAB_ERR_CUDA if the device reported an error.
+ */
+CPAB_API int cpab_device_status(unsigned *flags, int clear);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPAB_GB300_H */

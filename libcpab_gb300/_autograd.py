@@ -1,0 +1,155 @@
+"""torch.autograd.Function wrappers around the C ABI.
+
+TransformGrid  -- forward/backward of transformer (libcpab/pytorch/transformer.py:136-202)
+TransformGridNumeric -- forward differences in theta, the scheme the reference's
+                  numeric_grad option intends (libcpab/pytorch/transformer.py:205-295)
+Interpolate    -- interpolation with its backward (libcpab/pytorch/interpolation.py)
+TransformData  -- fused meshgrid -> integrate -> sample (libcpab/cpab.py:304-331)
+
+Gradient modes (params.gradient):
+  'reference' -- the reference's analytic gradient: the midpoint-rule
+                 sensitivity of libcpab/core/cpab_ops.cu:390-697, evaluated in
+                 reverse mode (default, for drop-in parity);
+  'exact'     -- the exact derivative of the forward map that was evaluated.
+"""
+from __future__ import annotations
+
+import torch
+from torch.autograd.function import once_differentiable
+
+from . import _native as N
+
+
+def _mode(params):
+    g = getattr(params, 'gradient', 'reference')
+    if g not in ('reference', 'exact'):
+        raise ValueError("params.gradient must be 'reference' or 'exact' (got %r)" % (g,))
+    return N.GRAD_EXACT if g == 'exact' else N.GRAD_REFERENCE
+
+
+def _ties(params):
+    return getattr(params, 'tie_counter', None)
+
+
+def _basis(params, device):
+    from .functions import basis_on
+    return basis_on(params, device)
+
+
+class TransformGrid(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, points, theta, params):
+        points = points.detach().to(torch.float32).contiguous()
+        theta_c = theta.detach().to(torch.float32).contiguous()
+        basis = _basis(params, theta.device)
+        A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis)
+        out = N.integrate(params.nc, params.nstepsolver, points, E, ties=_ties(params))
+        ctx.save_for_backward(points, A, E)
+        ctx.params = params
+        ctx.points_dim = points.dim()
+        return out
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, grad):
+        points, A, E = ctx.saved_tensors
+        params = ctx.params
+        if not (ctx.needs_input_grad[0] or ctx.needs_input_grad[1]):
+            return None, None, None
+        dtheta, dpoints = N.backward(params.nc, params.nstepsolver, _mode(params), points, A, E,
+                                     _basis(params, points.device),
+                                     grad.to(torch.float32).contiguous(),
+                                     want_dpoints=ctx.needs_input_grad[0], ties=_ties(params))
+        if dpoints is not None and ctx.points_dim == 2:
+            dpoints = dpoints.sum(dim=0)
+        return dpoints, (dtheta if ctx.needs_input_grad[1] else None), None
+
+
+class TransformGridNumeric(torch.autograd.Function):
+    STEP = 0.01
+
+    @staticmethod
+    def forward(ctx, points, theta, params):
+        points = points.detach().to(torch.float32).contiguous()
+        theta_c = theta.detach().to(torch.float32).contiguous()
+        basis = _basis(params, theta.device)
+        _, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis, want_A=False)
+        out = N.integrate(params.nc, params.nstepsolver, points, E)
+        ctx.save_for_backward(points, theta_c, out)
+        ctx.params = params
+        return out
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, grad):
+        points, theta, out = ctx.saved_tensors
+        params = ctx.params
+        basis = _basis(params, theta.device)
+        h = TransformGridNumeric.STEP
+        cols = []
+        for k in range(theta.shape[1]):
+            t = theta.clone()
+            t[:, k] += h
+            _, _, E = N.cell_tables(params.nc, params.nstepsolver, t, basis, want_A=False)
+            o = N.integrate(params.nc, params.nstepsolver, points, E)
+            cols.append((grad * (o - out) / h).sum(dim=(1, 2)))
+        return None, torch.stack(cols, dim=1), None
+
+
+class Interpolate(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, data, grid, outsize):
+        data_c = data.detach().to(torch.float32).contiguous()
+        grid_c = grid.detach().to(torch.float32).contiguous()
+        out = N.interpolate(data_c, grid_c, outsize)
+        ctx.save_for_backward(data_c, grid_c)
+        ctx.outsize = outsize
+        return out
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, grad):
+        data, grid = ctx.saved_tensors
+        want_d, want_g = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        if not (want_d or want_g):
+            return None, None, None
+        ddata, dgrid = N.interpolate_backward(data, grid, ctx.outsize,
+                                              grad.to(torch.float32).contiguous(),
+                                              want_ddata=want_d, want_dgrid=want_g)
+        return ddata, dgrid, None
+
+
+class TransformData(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, data, theta, params, outsize):
+        data_c = data.detach().to(torch.float32).contiguous()
+        theta_c = theta.detach().to(torch.float32).contiguous()
+        dev = data.device
+        lin = torch.cat([torch.linspace(params.domain_min[i], params.domain_max[i], outsize[i],
+                                        device=dev) for i in range(params.ndim)]).contiguous()
+        basis = _basis(params, dev)
+        A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis)
+        mode = _mode(params)
+        needs_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
+        save_grid = needs_grad and mode == N.GRAD_REFERENCE
+        out, grid = N.transform_data(params.nc, params.nstepsolver, lin, outsize, E, data_c,
+                                     save_grid=save_grid, ties=_ties(params))
+        ctx.save_for_backward(data_c, lin, A, E, grid)
+        ctx.params = params
+        ctx.outsize = outsize
+        ctx.mode = mode
+        return out
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, grad):
+        data, lin, A, E, grid = ctx.saved_tensors
+        params = ctx.params
+        want_d, want_t = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        if not (want_d or want_t):
+            return None, None, None, None
+        ddata, dtheta = N.transform_data_backward(
+            params.nc, params.nstepsolver, ctx.mode, lin, ctx.outsize, A, E, grid, data,
+            _basis(params, data.device), grad.to(torch.float32).contiguous(), want_ddata=want_d,
+            ties=_ties(params))
+        return ddata, (dtheta if want_t else None), None, None

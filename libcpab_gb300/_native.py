@@ -1,0 +1,284 @@
+"""ctypes binding of the C ABI in include/cpab_gb300.h.
+
+The shared library libcpab_gb300/libcpab_gb300.so is built by
+libcpab_gb300/build.py.  There is no fallback: if the library is missing or
+fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libcpab_gb300.so')
+
+GRAD_REFERENCE = 0
+GRAD_EXACT = 1
+
+_c_int_p = ctypes.POINTER(ctypes.c_int)
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_ll = ctypes.c_longlong
+_sz = ctypes.c_size_t
+
+_SIGS = {
+    'cpab_last_error': ([], ctypes.c_char_p),
+    'cpab_version': ([], _i),
+    'cpab_num_cells': ([_i, _c_int_p], _i),
+    'cpab_cell_tables': ([_i, _c_int_p, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp], _i),
+    'cpab_forward': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _vp], _i),
+    'cpab_integrate': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _vp, _vp], _i),
+    'cpab_backward_workspace': ([_i, _c_int_p, _i, _ll, _i], _sz),
+    'cpab_backward': ([_i, _c_int_p, _i, _i, _vp, _i, _ll, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp,
+                       _vp, _sz, _vp, _vp], _i),
+    'cpab_interpolate': ([_i, _vp, _i, _i, _c_int_p, _vp, _c_int_p, _vp, _vp], _i),
+    'cpab_interpolate_backward': ([_i, _vp, _i, _i, _c_int_p, _vp, _c_int_p, _vp, _vp, _vp, _vp],
+                                  _i),
+    'cpab_transform_data': ([_i, _c_int_p, _i, _vp, _c_int_p, _vp, _i, _vp, _i, _c_int_p, _vp,
+                             _vp, _vp, _vp], _i),
+    'cpab_transform_data_backward_workspace': ([_i, _c_int_p, _i, _i, _c_int_p, _i], _sz),
+    'cpab_transform_data_backward': ([_i, _c_int_p, _i, _i, _vp, _c_int_p, _vp, _vp, _vp, _i, _vp,
+                                      _i, _c_int_p, _vp, _i, _vp, _vp, _vp, _vp, _sz, _vp, _vp],
+                                     _i),
+    'cpab_findcellidx': ([_i, _c_int_p, _vp, _ll, _vp, _vp, _vp], _i),
+    'cpab_device_status': ([ctypes.POINTER(ctypes.c_uint), _i], _i),
+}
+
+EXPORTED = tuple(_SIGS)
+
+_lib = None
+_lock = threading.Lock()
+
+
+class CpabError(RuntimeError):
+    """Raised when a C-ABI call returns an error status."""
+
+
+def load(path: str | None = None):
+    """Load (once) and return the shared library.  Raises if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    with _lock:
+        if _lib is not None and path is None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise ImportError(
+                'libcpab_gb300 native library not found at %s; build it with '
+                '"python -m libcpab_gb300.build" (there is no CPU fallback)' % p)
+        lib = ctypes.CDLL(p)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        if path is None:
+            _lib = lib
+        return lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        msg = load().cpab_last_error().decode(errors='replace')
+        raise CpabError('libcpab_gb300 error %d: %s' % (rc, msg))
+
+
+def _ints(v):
+    v = [int(x) for x in v]
+    return (ctypes.c_int * len(v))(*v)
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(device) -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _require(t, name, dtype=torch.float32):
+    if not isinstance(t, torch.Tensor):
+        raise TypeError('%s must be a torch.Tensor' % name)
+    if not t.is_cuda:
+        raise ValueError('%s must be a CUDA tensor (no CPU fallback)' % name)
+    if t.dtype != dtype:
+        raise TypeError('%s must be %s (got %s)' % (name, dtype, t.dtype))
+    if not t.is_contiguous():
+        raise ValueError('%s must be contiguous' % name)
+
+
+# ----------------------------------------------------------------------------- #
+def num_cells(nc) -> int:
+    n = load().cpab_num_cells(len(nc), _ints(nc))
+    if n < 0:
+        _check(1)
+    return n
+
+
+def cell_tables(nc, nsteps, theta, basis, want_A=True, want_T=False, want_E=True):
+    """theta [n_theta, d], basis [D, d] (device fp32) -> (A, T, E) tables."""
+    _require(theta, 'theta')
+    _require(basis, 'basis')
+    ndim = len(nc)
+    n_theta, d = theta.shape
+    nC = num_cells(nc)
+    shape = (n_theta, nC, ndim, ndim + 1)
+    mk = lambda w: torch.empty(shape, device=theta.device, dtype=torch.float32) if w else None
+    A, T, E = mk(want_A), mk(want_T), mk(want_E)
+    _check(load().cpab_cell_tables(ndim, _ints(nc), int(nsteps), _ptr(theta), n_theta, d,
+                                   _ptr(basis), _ptr(A), _ptr(T), _ptr(E), _stream(theta.device)))
+    return A, T, E
+
+
+def forward_trels(nc, nsteps, points, trels):
+    """Reference-layout step maps T: drop-in for cpab_gpu.forward."""
+    _require(points, 'points')
+    _require(trels, 'trels')
+    ndim = len(nc)
+    n_theta = trels.shape[0]
+    broadcast = int(points.dim() == 3 and points.shape[0] == n_theta)
+    nP = points.shape[-1]
+    out = torch.empty((n_theta, ndim, nP), device=points.device, dtype=torch.float32)
+    _check(load().cpab_forward(ndim, _ints(nc), int(nsteps), _ptr(points), broadcast, nP,
+                               _ptr(trels), n_theta, _ptr(out), _stream(points.device)))
+    return out
+
+
+def integrate(nc, nsteps, points, E, ties=None):
+    _require(points, 'points')
+    _require(E, 'E')
+    ndim = len(nc)
+    n_theta = E.shape[0]
+    broadcast = int(points.dim() == 3 and points.shape[0] == n_theta)
+    nP = points.shape[-1]
+    out = torch.empty((n_theta, ndim, nP), device=points.device, dtype=torch.float32)
+    _check(load().cpab_integrate(ndim, _ints(nc), int(nsteps), _ptr(points), broadcast, nP,
+                                 _ptr(E), n_theta, _ptr(out), _ptr(ties), _stream(points.device)))
+    return out
+
+
+def backward(nc, nsteps, mode, points, A, E, basis, grad_out, want_dpoints=False, ties=None,
+             workspace=None):
+    """dtheta [n_theta, d] (and dL/dpoints per theta) from dL/d(out)."""
+    _require(points, 'points')
+    _require(A, 'A')
+    _require(basis, 'basis')
+    _require(grad_out, 'grad_out')
+    if mode == GRAD_EXACT:
+        _require(E, 'E')
+    ndim = len(nc)
+    n_theta = A.shape[0]
+    d = basis.shape[1]
+    broadcast = int(points.dim() == 3 and points.shape[0] == n_theta)
+    nP = points.shape[-1]
+    dev = points.device
+    dtheta = torch.empty((n_theta, d), device=dev, dtype=torch.float32)
+    dpoints = torch.empty((n_theta, ndim, nP), device=dev, dtype=torch.float32) \
+        if want_dpoints else None
+    lib = load()
+    need = lib.cpab_backward_workspace(ndim, _ints(nc), int(nsteps), nP, n_theta)
+    if need == 0 and nP > 0 and n_theta > 0:
+        _check(3)
+    if workspace is None or workspace.numel() < need:
+        workspace = torch.empty(max(need, 1), device=dev, dtype=torch.uint8)
+    _check(lib.cpab_backward(ndim, _ints(nc), int(nsteps), int(mode), _ptr(points), broadcast, nP,
+                             _ptr(A), _ptr(E), n_theta, _ptr(basis), d, _ptr(grad_out),
+                             _ptr(dtheta), _ptr(dpoints), _ptr(workspace), workspace.numel(),
+                             _ptr(ties), _stream(dev)))
+    return dtheta, dpoints
+
+
+def interpolate(data, grid, outsize):
+    _require(data, 'data')
+    _require(grid, 'grid')
+    ndim = grid.shape[1]
+    nb, C = data.shape[0], data.shape[1]
+    out = torch.empty((nb, C, *[int(o) for o in outsize]), device=data.device,
+                      dtype=torch.float32)
+    _check(load().cpab_interpolate(ndim, _ptr(data), nb, C, _ints(data.shape[2:]), _ptr(grid),
+                                   _ints(outsize), _ptr(out), _stream(data.device)))
+    return out
+
+
+def interpolate_backward(data, grid, outsize, grad_out, want_ddata=True, want_dgrid=True):
+    _require(data, 'data')
+    _require(grid, 'grid')
+    _require(grad_out, 'grad_out')
+    ndim = grid.shape[1]
+    nb, C = data.shape[0], data.shape[1]
+    ddata = torch.empty_like(data) if want_ddata else None
+    dgrid = torch.empty_like(grid) if want_dgrid else None
+    _check(load().cpab_interpolate_backward(ndim, _ptr(data), nb, C, _ints(data.shape[2:]),
+                                            _ptr(grid), _ints(outsize), _ptr(grad_out),
+                                            _ptr(ddata), _ptr(dgrid), _stream(data.device)))
+    return ddata, dgrid
+
+
+def transform_data(nc, nsteps, lin, outsize, E, data, save_grid=False, ties=None):
+    _require(lin, 'lin')
+    _require(E, 'E')
+    _require(data, 'data')
+    ndim = len(nc)
+    nb, C = data.shape[0], data.shape[1]
+    nP = 1
+    for o in outsize:
+        nP *= int(o)
+    out = torch.empty((nb, C, *[int(o) for o in outsize]), device=data.device,
+                      dtype=torch.float32)
+    grid = torch.empty((nb, ndim, nP), device=data.device, dtype=torch.float32) \
+        if save_grid else None
+    _check(load().cpab_transform_data(ndim, _ints(nc), int(nsteps), _ptr(lin), _ints(outsize),
+                                      _ptr(E), nb, _ptr(data), C, _ints(data.shape[2:]),
+                                      _ptr(out), _ptr(grid), _ptr(ties), _stream(data.device)))
+    return out, grid
+
+
+def transform_data_backward(nc, nsteps, mode, lin, outsize, A, E, grid_saved, data, basis,
+                            grad_out, want_ddata=True, ties=None, workspace=None):
+    _require(lin, 'lin')
+    _require(A, 'A')
+    _require(data, 'data')
+    _require(basis, 'basis')
+    _require(grad_out, 'grad_out')
+    if mode == GRAD_EXACT:
+        _require(E, 'E')
+    else:
+        _require(grid_saved, 'grid_saved')
+    ndim = len(nc)
+    nb, C = data.shape[0], data.shape[1]
+    d = basis.shape[1]
+    dev = data.device
+    dtheta = torch.empty((nb, d), device=dev, dtype=torch.float32)
+    ddata = torch.empty_like(data) if want_ddata else None
+    lib = load()
+    need = lib.cpab_transform_data_backward_workspace(ndim, _ints(nc), int(nsteps), int(mode),
+                                                      _ints(outsize), nb)
+    if need == 0 and nb > 0:
+        _check(3)
+    if workspace is None or workspace.numel() < need:
+        workspace = torch.empty(max(need, 1), device=dev, dtype=torch.uint8)
+    _check(lib.cpab_transform_data_backward(
+        ndim, _ints(nc), int(nsteps), int(mode), _ptr(lin), _ints(outsize), _ptr(A), _ptr(E),
+        _ptr(grid_saved), nb, _ptr(data), C, _ints(data.shape[2:]), _ptr(basis), d,
+        _ptr(grad_out), _ptr(ddata), _ptr(dtheta), _ptr(workspace), workspace.numel(),
+        _ptr(ties), _stream(dev)))
+    return ddata, dtheta
+
+
+def findcellidx(nc, points, ties=None):
+    _require(points, 'points')
+    ndim = len(nc)
+    nP = points.shape[-1]
+    out = torch.empty((nP,), device=points.device, dtype=torch.int32)
+    _check(load().cpab_findcellidx(ndim, _ints(nc), _ptr(points), nP, _ptr(out), _ptr(ties),
+                                   _stream(points.device)))
+    return out
+
+
+def device_status(clear=True) -> int:
+    flags = ctypes.c_uint(0)
+    _check(load().cpab_device_status(ctypes.byref(flags), int(bool(clear))))
+    return flags.value

@@ -1,0 +1,352 @@
+// Backward of the integration: dL/dtheta (and dL/dpoints) from dL/d(out).
+//
+// The reference (libcpab/core/cpab_ops.cu:390-697, launched from
+// libcpab/pytorch/transformer_cuda.cu:66-119) runs one thread per
+// (point, theta, basis index k), integrates the midpoint-rule sensitivity
+// q_k = d p / d theta_k for every k, writes the full [d, n_theta, ndim, nP]
+// tensor (read-modify-written at each of the nsteps steps) and contracts it
+// with the cotangent in Python (libcpab/pytorch/transformer.py:201).  Its cost
+// grows with d and its memory is d * n_theta * ndim * nP floats.
+//
+// Here one thread owns one trajectory and pushes the cotangent backwards
+// through the visited cells (reverse mode), so the cost is independent of d:
+//
+//   mode 0 ("reference"): the transpose of the reference's own recurrence.
+//     The reference integrates, along the midpoint trajectory
+//     pMid = p + h/2 A[p;1],  p' = p + h A[pMid;1],
+//     q' = M q + h B_k [pMid;1] + h^2/2 A B_k [p;1],  M = I + hA + h^2/2 A^2,
+//     so with lambda_N = dL/dp_N and lambda_n = M^T lambda_{n+1}:
+//     dL/dtheta_k = sum_n < B_k,c_n , G_n >,
+//     G_n = h lambda_{n+1} [pMid_n;1]^T + h^2/2 (A^T lambda_{n+1}) [p_n;1]^T.
+//     The result is the reference's analytic gradient up to rounding.
+//   mode 1 ("exact"): exact discrete adjoint of the forward map
+//     p' = p + E_c [p;1]:  dL/dT_c += lambda_{n+1} [p_n;1]^T,
+//     lambda_n = lambda_{n+1} + E_lin^T lambda_{n+1}; dL/dA then follows from
+//     the adjoint Frechet derivative of expm (k_finalize).
+//
+// No per-step state goes to global memory: the forward pass logs each step's
+// cell (1 or 2 bytes) and a checkpoint every S steps in shared memory; the
+// reverse pass rebuilds each segment's positions from its checkpoint with the
+// logged cells (no cell lookups) into registers.
+//
+// Deterministic reduction: a thread accumulates its contribution for the
+// current cell in registers and flushes it when the cell changes.  Flushing
+// lanes of a warp are grouped by cell (match.any); each group is reduced with
+// shuffles in a fixed order and its leader adds the sum into the warp's own
+// copy of the cell-gradient table in shared memory.  At the end the warp
+// copies are summed in warp order into one partial per CTA, and k_finalize
+// sums the partials in CTA order.  No floating-point atomics are used, so the
+// result is bit-reproducible for a given GPU and input.
+#include "cpab_adjoint.cuh"
+
+namespace cpab {
+
+template <int N, int MODE, typename CT>
+__global__ void __launch_bounds__(256)
+    k_adjoint(Tess t, int nsteps, Steps st, const float *__restrict__ points, int broadcast,
+              long long nP, const float *__restrict__ table, int parts, int tiles,
+              const float *__restrict__ gout, float *__restrict__ dpoints,
+              float *__restrict__ partials, unsigned long long *ties, unsigned *err) {
+    constexpr int P = N * (N + 1);
+    extern __shared__ float4 smem4[];
+    __shared__ uint64_t bar;
+    const int B = blockDim.x, tid = threadIdx.x, W = B / 32;
+    const int G = t.nC * P, Gr = round4(G);
+    const int nseg = (nsteps + kSeg - 1) / kSeg;
+    float *tab = reinterpret_cast<float *>(smem4);
+    float *gw = tab + Gr;
+    float *ck = gw + (size_t)W * Gr;
+    CT *cl = reinterpret_cast<CT *>(ck + (size_t)nseg * N * B);
+
+    const int th = blockIdx.x / parts, part = blockIdx.x % parts;
+    if (!stage_table(tab, table + (long long)th * G, G, &bar, err)) return;
+    for (int i = tid; i < W * Gr; i += B) gw[i] = 0.f;
+    __syncthreads();
+    float *warp_tab = gw + (size_t)(tid >> 5) * Gr;
+    const float *src = points + (broadcast ? (long long)th * N * nP : 0ll);
+
+    for (int tile = part; tile < tiles; tile += parts) {
+        const long long idx = (long long)tile * B + tid;
+        const bool live = idx < nP;
+        float p[N], lam[N];
+#pragma unroll
+        for (int r = 0; r < N; ++r) p[r] = live ? __ldg(src + r * nP + idx) : 0.5f;
+        logged_forward<N, MODE, CT>(tab, t, nsteps, st, p, ck, cl, ties, err);
+#pragma unroll
+        for (int r = 0; r < N; ++r) lam[r] = live ? __ldg(gout + ((long long)th * N + r) * nP + idx) : 0.f;
+        reverse_sweep<N, MODE, CT>(tab, ck, cl, nsteps, st, live, lam, warp_tab);
+        if (dpoints && live) {
+#pragma unroll
+            for (int r = 0; r < N; ++r) dpoints[((long long)th * N + r) * nP + idx] = lam[r];
+        }
+    }
+    __syncthreads();
+    float *dst = partials + ((long long)th * parts + part) * G;
+    for (int i = tid; i < G; i += B) {
+        float s = 0.f;
+        for (int w = 0; w < W; ++w) s += gw[(size_t)w * Gr + i];
+        dst[i] = s;
+    }
+}
+
+// ------------------------------ planning -------------------------------------
+template <int N, int MODE, typename CT>
+static bool plan_t(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan) {
+    int dev = 0, max_optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (max_optin <= 0) max_optin = 48 * 1024;
+    const int cands[3] = {256, 128, 64};
+    for (int ci = 0; ci < 3; ++ci) {
+        const int block = cands[ci];
+        const size_t smem = adjoint_smem_bytes<N, CT>(t.nC, nsteps, block) + 64;
+        if (smem > (size_t)max_optin) continue;
+        auto kern = k_adjoint<N, MODE, CT>;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return false;
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
+        if (per_sm <= 0) continue;
+        const long long tiles = (nP + block - 1) / block;
+        const long long target = 2ll * num_sms() * per_sm;
+        long long parts = (target + n_theta - 1) / n_theta;
+        if (parts > tiles) parts = tiles;
+        if (parts < 1) parts = 1;
+        plan->block = block;
+        plan->tiles = (int)tiles;
+        plan->parts = (int)parts;
+        plan->smem = smem;
+        plan->partial_floats = (size_t)n_theta * parts * t.nC * N * (N + 1);
+        return true;
+    }
+    return false;
+}
+
+bool plan_adjoint_mode(const Tess &t, int nsteps, int mode, long long nP, int n_theta,
+                       AdjointPlan *plan) {
+    const bool small = t.nC <= 256;
+#define CPAB_PLAN(N)                                                                          \
+    if (mode == 0)                                                                            \
+        return small ? plan_t<N, 0, uint8_t>(t, nsteps, nP, n_theta, plan)                    \
+                     : plan_t<N, 0, uint16_t>(t, nsteps, nP, n_theta, plan);                  \
+    return small ? plan_t<N, 1, uint8_t>(t, nsteps, nP, n_theta, plan)                        \
+                 : plan_t<N, 1, uint16_t>(t, nsteps, nP, n_theta, plan);
+    switch (t.ndim) {
+        case 1: { CPAB_PLAN(1) }
+        case 2: { CPAB_PLAN(2) }
+        default: { CPAB_PLAN(3) }
+    }
+#undef CPAB_PLAN
+}
+
+bool plan_adjoint(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan) {
+    // Both modes share the shared-memory layout; plan with the larger register
+    // footprint (mode 0) so the plan is valid for either.
+    return plan_adjoint_mode(t, nsteps, 0, nP, n_theta, plan);
+}
+
+template <int N, int MODE, typename CT>
+static cudaError_t launch_adjoint_t(const Tess &t, int nsteps, const AdjointPlan &plan,
+                                    const float *points, int broadcast, long long nP,
+                                    const float *table, int n_theta, const float *gout,
+                                    float *dpoints, float *partials, unsigned long long *ties,
+                                    unsigned *err, cudaStream_t s) {
+    auto kern = k_adjoint<N, MODE, CT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)plan.smem);
+    if (e != cudaSuccess) return e;
+    Steps st;
+    st.h = (float)(1.0 / nsteps);
+    st.hh = (float)(0.5 / nsteps);
+    st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
+    const long long grid = (long long)n_theta * plan.parts;
+    if (grid == 0) return cudaSuccess;
+    kern<<<(unsigned)grid, plan.block, plan.smem, s>>>(t, nsteps, st, points, broadcast, nP, table,
+                                                       plan.parts, plan.tiles, gout, dpoints,
+                                                       partials, ties, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const Tess &t, int nsteps, int mode, const AdjointPlan &plan,
+                           const float *points, int broadcast, long long nP, const float *table,
+                           int n_theta, const float *gout, float *dpoints, float *partials,
+                           unsigned long long *ties, unsigned *err, cudaStream_t s) {
+    const bool small = t.nC <= 256;
+#define CPAB_ADJ(N)                                                                             \
+    if (mode == 0)                                                                              \
+        return small ? launch_adjoint_t<N, 0, uint8_t>(t, nsteps, plan, points, broadcast, nP,  \
+                                                       table, n_theta, gout, dpoints, partials, \
+                                                       ties, err, s)                            \
+                     : launch_adjoint_t<N, 0, uint16_t>(t, nsteps, plan, points, broadcast, nP, \
+                                                        table, n_theta, gout, dpoints,          \
+                                                        partials, ties, err, s);                \
+    return small ? launch_adjoint_t<N, 1, uint8_t>(t, nsteps, plan, points, broadcast, nP,      \
+                                                   table, n_theta, gout, dpoints, partials,     \
+                                                   ties, err, s)                                \
+                 : launch_adjoint_t<N, 1, uint16_t>(t, nsteps, plan, points, broadcast, nP,     \
+                                                    table, n_theta, gout, dpoints, partials,    \
+                                                    ties, err, s);
+    switch (t.ndim) {
+        case 1: { CPAB_ADJ(1) }
+        case 2: { CPAB_ADJ(2) }
+        default: { CPAB_ADJ(3) }
+    }
+#undef CPAB_ADJ
+}
+
+// ------------------------------ finalize -------------------------------------
+// Frechet derivative of expm at Y in direction E, by a truncated Horner
+// recursion on Y/2^s, E/2^s followed by s squarings:
+//   R_{k-1} = I + (Y/k) R_k,  dR_{k-1} = (E/k) R_k + (Y/k) dR_k,
+//   then  L <- L R + R L,  R <- R R.
+template <int K>
+__device__ __forceinline__ void frechet_expm(const float (&Y0)[K][K], const float (&E0)[K][K],
+                                             float (&L)[K][K]) {
+    float norm = 0.f;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        float s = 0.f;
+#pragma unroll
+        for (int i = 0; i < K; ++i) s += fabsf(Y0[i][j]);
+        norm = fmaxf(norm, s);
+    }
+    int sq = 0;
+    if (norm > 0.5f) sq = min(64, (int)ceilf(log2f(norm / 0.5f)));
+    const float sc = ldexpf(1.f, -sq);
+    float Y[K][K], E[K][K], R[K][K], D[K][K];
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            Y[i][j] = Y0[i][j] * sc;
+            E[i][j] = E0[i][j] * sc;
+            R[i][j] = (i == j) ? 1.f : 0.f;
+            D[i][j] = 0.f;
+        }
+    for (int k = 12; k >= 1; --k) {
+        const float r = 1.f / (float)k;
+        float nR[K][K], nD[K][K];
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                float a = 0.f, b = 0.f;
+#pragma unroll
+                for (int m = 0; m < K; ++m) {
+                    a = fmaf(Y[i][m], R[m][j], a);
+                    b = fmaf(E[i][m], R[m][j], fmaf(Y[i][m], D[m][j], b));
+                }
+                nR[i][j] = fmaf(a, r, (i == j) ? 1.f : 0.f);
+                nD[i][j] = b * r;
+            }
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = 0; j < K; ++j) { R[i][j] = nR[i][j]; D[i][j] = nD[i][j]; }
+    }
+    for (int s = 0; s < sq; ++s) {
+        float nR[K][K], nD[K][K];
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                float a = 0.f, b = 0.f;
+#pragma unroll
+                for (int m = 0; m < K; ++m) {
+                    a = fmaf(R[i][m], R[m][j], a);
+                    b = fmaf(D[i][m], R[m][j], fmaf(R[i][m], D[m][j], b));
+                }
+                nR[i][j] = a;
+                nD[i][j] = b;
+            }
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = 0; j < K; ++j) { R[i][j] = nR[i][j]; D[i][j] = nD[i][j]; }
+    }
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+#pragma unroll
+        for (int j = 0; j < K; ++j) L[i][j] = D[i][j];
+}
+
+template <int N, int MODE>
+__global__ void __launch_bounds__(256)
+    k_finalize(int nC, float dt, const float *__restrict__ partials, int parts,
+               const float *__restrict__ A, const float *__restrict__ basis, int d,
+               float *__restrict__ dtheta) {
+    constexpr int P = N * (N + 1);
+    extern __shared__ float4 smem4[];
+    float *g = reinterpret_cast<float *>(smem4);
+    const int th = blockIdx.x, tid = threadIdx.x, B = blockDim.x;
+    const int G = nC * P;
+    const float *src = partials + (long long)th * parts * G;
+    for (int i = tid; i < G; i += B) {
+        float s = 0.f;
+        for (int q = 0; q < parts; ++q) s += __ldg(src + (long long)q * G + i);
+        g[i] = s;
+    }
+    __syncthreads();
+    if constexpr (MODE == 1) {
+        // dL/dT_c (top N rows) -> dL/dA_c = dt * [L_exp(X^T, [dL/dT_c; 0])]_{top rows}
+        for (int c = tid; c < nC; c += B) {
+            const float *a = A + ((long long)th * nC + c) * P;
+            float Y[N + 1][N + 1], E[N + 1][N + 1], L[N + 1][N + 1];
+#pragma unroll
+            for (int i = 0; i <= N; ++i)
+#pragma unroll
+                for (int j = 0; j <= N; ++j) {
+                    Y[j][i] = (i < N) ? dt * a[i * (N + 1) + j] : 0.f;   // Y = X^T
+                    E[i][j] = (i < N) ? g[c * P + i * (N + 1) + j] : 0.f;
+                }
+            frechet_expm<N + 1>(Y, E, L);
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+#pragma unroll
+                for (int j = 0; j <= N; ++j) g[c * P + i * (N + 1) + j] = dt * L[i][j];
+        }
+        __syncthreads();
+    }
+    for (int k = tid; k < d; k += B) {
+        float acc = 0.f;
+        for (int i = 0; i < G; ++i) acc = fmaf(__ldg(basis + (long long)i * d + k), g[i], acc);
+        dtheta[(long long)th * d + k] = acc;
+    }
+}
+
+cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *partials, int parts,
+                            const float *A, const float *basis, int d, int n_theta,
+                            float *dtheta, cudaStream_t s) {
+    if (n_theta == 0) return cudaSuccess;
+    const int P = t.ndim * (t.ndim + 1);
+    const size_t smem = (size_t)t.nC * P * sizeof(float);
+    const float dt = (float)(1.0 / nsteps);
+    const int block = 256;
+#define CPAB_FIN(N, M)                                                                         \
+    {                                                                                          \
+        auto kern = k_finalize<N, M>;                                                          \
+        if (smem > 48 * 1024) {                                                                \
+            cudaError_t e = cudaFuncSetAttribute(                                              \
+                kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                 \
+            if (e != cudaSuccess) return e;                                                    \
+        }                                                                                      \
+        kern<<<n_theta, block, smem, s>>>(t.nC, dt, partials, parts, A, basis, d, dtheta);     \
+        return cudaGetLastError();                                                             \
+    }
+    if (mode == 0) {
+        switch (t.ndim) {
+            case 1: CPAB_FIN(1, 0)
+            case 2: CPAB_FIN(2, 0)
+            default: CPAB_FIN(3, 0)
+        }
+    }
+    switch (t.ndim) {
+        case 1: CPAB_FIN(1, 1)
+        case 2: CPAB_FIN(2, 1)
+        default: CPAB_FIN(3, 1)
+    }
+#undef CPAB_FIN
+}
+
+}  // namespace cpab

@@ -1,0 +1,363 @@
+// extern "C" entry points declared in include/cpab_gb300.h: argument
+// validation, tessellation constants, error reporting, and dispatch to the
+// kernel launchers.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "../../include/cpab_gb300.h"
+#include "cpab_launch.h"
+
+using namespace cpab;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int fail(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return fail(CPAB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Device error word, one per device (file-scope __device__ variable; its
+// device address is looked up once per device).
+__device__ unsigned g_device_error;
+constexpr int kMaxDevices = 64;
+unsigned *g_err_ptr[kMaxDevices] = {nullptr};
+
+unsigned *device_error_word() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+    if (!g_err_ptr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_device_error) != cudaSuccess) return nullptr;
+        g_err_ptr[dev] = static_cast<unsigned *>(p);
+    }
+    return g_err_ptr[dev];
+}
+
+// Tessellation constants, computed the way the reference computes them
+// (libcpab/core/cpab_ops.cpp:40-45, 108-110, 139-141).
+int make_tess(int ndim, const int *nc, Tess *t) {
+    if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3 (got %d)", ndim);
+    if (!nc) return fail(CPAB_ERR_ARGUMENT, "nc is NULL");
+    long long ncells = 1;
+    int ncmax = 1;
+    for (int j = 0; j < ndim; ++j) {
+        if (nc[j] < 1 || nc[j] > 4096)
+            return fail(CPAB_ERR_ARGUMENT, "nc[%d] = %d out of range [1, 4096]", j, nc[j]);
+        ncells *= nc[j];
+        ncmax = nc[j] > ncmax ? nc[j] : ncmax;
+    }
+    ncells *= (ndim == 1 ? 1 : ndim == 2 ? 4 : 5);
+    if (ncells > 65535) return fail(CPAB_ERR_UNSUPPORTED, "too many cells (%lld > 65535)", ncells);
+    memset(t, 0, sizeof(*t));
+    t->ndim = ndim;
+    for (int j = 0; j < 3; ++j) {
+        const int n = j < ndim ? nc[j] : 1;
+        t->nc[j] = n;
+        t->inc[j] = (float)(1.0 / n);
+        t->rinc[j] = (float)(1.0 / (double)t->inc[j]);
+        t->wlim[j] = (float)n * t->inc[j];
+    }
+    t->nC = (int)ncells;
+    if (ndim == 3) {
+        t->clamp3[0] = (float)((double)((float)nc[0] * t->inc[0]) - 1e-8);
+        t->clamp3[1] = (float)((double)((float)nc[1] * t->inc[1]) - 1e-8);
+        t->clamp3[2] = (float)((double)((float)nc[2] * t->inc[0]) - 1e-8);  // inc_x, as the reference
+        for (int j = 0; j < 3; ++j) t->lim3[j] = t->clamp3[j] < 1.0f ? t->clamp3[j] : 1.0f;
+    }
+    t->eps = (float)((8.0 * ncmax + 16.0) * ldexp(1.0, -23));
+    return CPAB_OK;
+}
+
+int check_steps(int nsteps) {
+    if (nsteps < 1 || nsteps > 100000)
+        return fail(CPAB_ERR_ARGUMENT, "nsteps must be in [1, 100000] (got %d)", nsteps);
+    return CPAB_OK;
+}
+
+cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int check_sizes(int ndim, const int *v, const char *name) {
+    if (!v) return fail(CPAB_ERR_ARGUMENT, "%s is NULL", name);
+    for (int j = 0; j < ndim; ++j)
+        if (v[j] < 1) return fail(CPAB_ERR_ARGUMENT, "%s[%d] = %d must be positive", name, j, v[j]);
+    return CPAB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cpab_last_error(void) { return g_err; }
+
+int cpab_version(void) { return 10000; }
+
+int cpab_num_cells(int ndim, const int *nc) {
+    Tess t;
+    if (make_tess(ndim, nc, &t) != CPAB_OK) return -1;
+    return t.nC;
+}
+
+int cpab_cell_tables(int ndim, const int *nc, int nsteps, const float *theta, int n_theta,
+                     int d, const float *basis, float *A, float *T, float *E, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if (n_theta < 0 || d < 0) return fail(CPAB_ERR_ARGUMENT, "need n_theta >= 0 and d >= 0");
+    if (n_theta > 0 && d > 0 && (!theta || !basis))
+        return fail(CPAB_ERR_ARGUMENT, "theta or basis is NULL");
+    cudaError_t e = launch_cell_tables(t, nsteps, theta, n_theta, d, basis, A, T, E, as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "cell tables launch");
+}
+
+static int integrate_common(int ndim, const int *nc, int nsteps, const float *points,
+                            int broadcast, long long nP, const float *table, bool comp,
+                            int n_theta, float *out, unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if (nP < 0 || n_theta < 0) return fail(CPAB_ERR_ARGUMENT, "negative size");
+    if (nP == 0 || n_theta == 0) return CPAB_OK;
+    if (!points || !table || !out) return fail(CPAB_ERR_ARGUMENT, "points, table or out is NULL");
+    unsigned *err = device_error_word();
+    cudaError_t e = launch_integrate(t, nsteps, points, broadcast ? 1 : 0, nP, table, comp, n_theta,
+                                     out, ties, err, as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "integrate launch");
+}
+
+int cpab_forward(int ndim, const int *nc, int nsteps, const float *points, int broadcast,
+                 long long nP, const float *trels, int n_theta, float *out, void *stream) {
+    return integrate_common(ndim, nc, nsteps, points, broadcast, nP, trels, false, n_theta, out,
+                            nullptr, stream);
+}
+
+int cpab_integrate(int ndim, const int *nc, int nsteps, const float *points, int broadcast,
+                   long long nP, const float *E, int n_theta, float *out,
+                   unsigned long long *ties, void *stream) {
+    return integrate_common(ndim, nc, nsteps, points, broadcast, nP, E, true, n_theta, out, ties,
+                            stream);
+}
+
+size_t cpab_backward_workspace(int ndim, const int *nc, int nsteps, long long nP, int n_theta) {
+    g_err[0] = 0;
+    Tess t;
+    if (make_tess(ndim, nc, &t) || check_steps(nsteps)) return 0;
+    if (nP <= 0 || n_theta <= 0) return 0;
+    AdjointPlan plan;
+    if (!plan_adjoint(t, nsteps, nP, n_theta, &plan)) {
+        fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
+        return 0;
+    }
+    return plan.partial_floats * sizeof(float);
+}
+
+int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *points,
+                  int broadcast, long long nP, const float *A, const float *E, int n_theta,
+                  const float *basis, int d, const float *grad_out, float *dtheta,
+                  float *dpoints, void *workspace, size_t workspace_bytes,
+                  unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+        return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
+    if (nP < 0 || n_theta < 0 || d < 0) return fail(CPAB_ERR_ARGUMENT, "invalid sizes");
+    if (n_theta == 0 || (d == 0 && !dpoints)) return CPAB_OK;   // nothing to compute
+    if (!A || (d > 0 && (!dtheta || !basis)))
+        return fail(CPAB_ERR_ARGUMENT, "dtheta, basis or A is NULL");
+    if (mode == CPAB_GRAD_EXACT && !E) return fail(CPAB_ERR_ARGUMENT, "exact mode needs E");
+    cudaStream_t s = as_stream(stream);
+    if (nP == 0) {
+        cudaError_t e = cudaMemsetAsync(dtheta, 0, (size_t)n_theta * d * sizeof(float), s);
+        return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "memset");
+    }
+    if (!points || !grad_out) return fail(CPAB_ERR_ARGUMENT, "points or grad_out is NULL");
+    AdjointPlan plan;
+    if (!plan_adjoint(t, nsteps, nP, n_theta, &plan))
+        return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
+    const size_t need = plan.partial_floats * sizeof(float);
+    if (!workspace || workspace_bytes < need)
+        return fail(CPAB_ERR_WORKSPACE, "workspace of %zu bytes needed (got %zu)", need,
+                    workspace ? workspace_bytes : (size_t)0);
+    float *partials = static_cast<float *>(workspace);
+    unsigned *err = device_error_word();
+    cudaError_t e = launch_adjoint(t, nsteps, mode, plan, points, broadcast ? 1 : 0, nP,
+                                   mode == CPAB_GRAD_EXACT ? E : A, n_theta, grad_out, dpoints,
+                                   partials, ties, err, s);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+    if (d == 0) return CPAB_OK;
+    e = launch_finalize(t, nsteps, mode, partials, plan.parts, A, basis, d, n_theta, dtheta, s);
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "finalize launch");
+}
+
+int cpab_interpolate(int ndim, const float *data, int nb, int C, const int *size,
+                     const float *grid, const int *outsize, float *out, void *stream) {
+    g_err[0] = 0;
+    if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3");
+    int rc;
+    if ((rc = check_sizes(ndim, size, "size")) || (rc = check_sizes(ndim, outsize, "outsize")))
+        return rc;
+    if (nb < 0 || C < 1) return fail(CPAB_ERR_ARGUMENT, "invalid nb or C");
+    if (nb == 0) return CPAB_OK;
+    if (!data || !grid || !out) return fail(CPAB_ERR_ARGUMENT, "data, grid or out is NULL");
+    cudaError_t e = launch_interpolate(ndim, data, nb, C, size, grid, outsize, out, as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "interpolate launch");
+}
+
+int cpab_interpolate_backward(int ndim, const float *data, int nb, int C, const int *size,
+                              const float *grid, const int *outsize, const float *grad_out,
+                              float *ddata, float *dgrid, void *stream) {
+    g_err[0] = 0;
+    if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3");
+    int rc;
+    if ((rc = check_sizes(ndim, size, "size")) || (rc = check_sizes(ndim, outsize, "outsize")))
+        return rc;
+    if (nb < 0 || C < 1) return fail(CPAB_ERR_ARGUMENT, "invalid nb or C");
+    if (nb == 0) return CPAB_OK;
+    if (!data || !grid || !grad_out) return fail(CPAB_ERR_ARGUMENT, "data, grid or grad_out is NULL");
+    cudaStream_t s = as_stream(stream);
+    if (ddata) {
+        size_t n = (size_t)nb * C;
+        for (int j = 0; j < ndim; ++j) n *= (size_t)size[j];
+        cudaError_t e = cudaMemsetAsync(ddata, 0, n * sizeof(float), s);
+        if (e != cudaSuccess) return cuda_fail(e, "memset");
+    }
+    cudaError_t e = launch_interpolate_backward(ndim, data, nb, C, size, grid, outsize, grad_out,
+                                                ddata, dgrid, s);
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "interpolate backward launch");
+}
+
+int cpab_transform_data(int ndim, const int *nc, int nsteps, const float *lin,
+                        const int *outsize, const float *E, int nb, const float *data, int C,
+                        const int *size, float *out, float *grid_out,
+                        unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if ((rc = check_sizes(ndim, size, "size")) || (rc = check_sizes(ndim, outsize, "outsize")))
+        return rc;
+    if (nb < 0 || C < 1) return fail(CPAB_ERR_ARGUMENT, "invalid nb or C");
+    if (nb == 0) return CPAB_OK;
+    if (!lin || !E || !data || !out) return fail(CPAB_ERR_ARGUMENT, "lin, E, data or out is NULL");
+    cudaError_t e = launch_transform_data(t, nsteps, lin, outsize, E, nb, data, C, size, out,
+                                          grid_out, ties, device_error_word(), as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "transform_data launch");
+}
+
+size_t cpab_transform_data_backward_workspace(int ndim, const int *nc, int nsteps, int mode,
+                                              const int *outsize, int nb) {
+    g_err[0] = 0;
+    Tess t;
+    if (make_tess(ndim, nc, &t) || check_steps(nsteps) || check_sizes(ndim, outsize, "outsize"))
+        return 0;
+    if (nb <= 0 || (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)) return 0;
+    long long nP = 1;
+    for (int j = 0; j < ndim; ++j) nP *= outsize[j];
+    AdjointPlan plan;
+    if (!plan_transform_data_backward(t, nsteps, mode, nP, nb, &plan)) {
+        fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
+        return 0;
+    }
+    return plan.partial_floats * sizeof(float);
+}
+
+int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, int mode,
+                                 const float *lin, const int *outsize, const float *A,
+                                 const float *E, const float *grid_saved, int nb,
+                                 const float *data, int C, const int *size, const float *basis,
+                                 int d, const float *grad_out, float *ddata, float *dtheta,
+                                 void *workspace, size_t workspace_bytes,
+                                 unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if ((rc = check_sizes(ndim, size, "size")) || (rc = check_sizes(ndim, outsize, "outsize")))
+        return rc;
+    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+        return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
+    if (nb < 0 || C < 1 || d < 0) return fail(CPAB_ERR_ARGUMENT, "invalid nb, C or d");
+    if (nb == 0) return CPAB_OK;
+    if (!lin || !A || !data || !grad_out || (d > 0 && (!basis || !dtheta)))
+        return fail(CPAB_ERR_ARGUMENT, "lin, A, data, basis, grad_out or dtheta is NULL");
+    if (mode == CPAB_GRAD_EXACT && !E) return fail(CPAB_ERR_ARGUMENT, "exact mode needs E");
+    if (mode == CPAB_GRAD_REFERENCE && !grid_saved)
+        return fail(CPAB_ERR_ARGUMENT, "reference mode needs grid_saved");
+    long long nP = 1;
+    for (int j = 0; j < ndim; ++j) nP *= outsize[j];
+    AdjointPlan plan;
+    if (!plan_transform_data_backward(t, nsteps, mode, nP, nb, &plan))
+        return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
+    const size_t need = plan.partial_floats * sizeof(float);
+    if (!workspace || workspace_bytes < need)
+        return fail(CPAB_ERR_WORKSPACE, "workspace of %zu bytes needed (got %zu)", need,
+                    workspace ? workspace_bytes : (size_t)0);
+    cudaStream_t s = as_stream(stream);
+    if (ddata) {
+        size_t n = (size_t)nb * C;
+        for (int j = 0; j < ndim; ++j) n *= (size_t)size[j];
+        cudaError_t e = cudaMemsetAsync(ddata, 0, n * sizeof(float), s);
+        if (e != cudaSuccess) return cuda_fail(e, "memset");
+    }
+    float *partials = static_cast<float *>(workspace);
+    cudaError_t e = launch_transform_data_backward(
+        t, nsteps, mode, plan, lin, outsize, mode == CPAB_GRAD_EXACT ? E : A, grid_saved, nb, data,
+        C, size, grad_out, ddata, partials, ties, device_error_word(), s);
+    if (e != cudaSuccess) return cuda_fail(e, "transform_data backward launch");
+    if (d == 0) return CPAB_OK;
+    e = launch_finalize(t, nsteps, mode, partials, plan.parts, A, basis, d, nb, dtheta, s);
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "finalize launch");
+}
+
+int cpab_findcellidx(int ndim, const int *nc, const float *points, long long nP, int *out,
+                     unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if (nP < 0) return fail(CPAB_ERR_ARGUMENT, "negative nP");
+    if (nP == 0) return CPAB_OK;
+    if (!points || !out) return fail(CPAB_ERR_ARGUMENT, "points or out is NULL");
+    cudaError_t e = launch_findcellidx(t, points, nP, out, ties, as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "findcellidx launch");
+}
+
+int cpab_device_status(unsigned *flags, int clear) {
+    g_err[0] = 0;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "device synchronize");
+    unsigned *p = device_error_word();
+    unsigned v = 0;
+    if (p) {
+        e = cudaMemcpy(&v, p, sizeof(v), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "read device error word");
+        if (clear) {
+            e = cudaMemset(p, 0, sizeof(unsigned));
+            if (e != cudaSuccess) return cuda_fail(e, "clear device error word");
+        }
+    }
+    if (flags) *flags = v;
+    return CPAB_OK;
+}
+
+}  // extern "C"

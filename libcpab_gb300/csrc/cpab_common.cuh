@@ -1,0 +1,332 @@
+// Shared device code for the CPAB integration kernels (sm_103a).
+//
+// Cell lookup
+// -----------
+// The reference decides the cell of a point in double precision
+// (libcpab/core/cpab_ops.cu:21-227 for CUDA, libcpab/core/cpab_ops.cpp:26-184
+// for the CPU).  GB300 has a low FP64 rate, so lookups here run in FP32 and
+// are *certified*: the FP32 quantities (cell coordinate q = p/inc, its
+// fractional parts, and the sub-cell plane tests) carry a proven error bound
+// (|error| <= nc * 2^-23 for q in [0,nc]).  When every quantity that decides
+// the cell is farther than eps = 8*nc*2^-23 from its threshold, the FP32
+// decision equals the reference's double decision.  Otherwise (and for every
+// point outside the unit box, where the reference's out-of-domain rules
+// apply) the lookup is redone with an FP64 replica of the reference's
+// arithmetic.  The result is bit-identical to the reference lookup for every
+// float input; the FP64 branch is taken for a fraction ~1e-5 of in-domain
+// lookups and is counted when a counter is supplied.
+//
+// Tables
+// ------
+// Per-theta cell tables use the reference's dense layout
+// [n_theta, nC, ndim, ndim+1] (row-major affine maps), for A (velocity),
+// T = expm(dt*A) (step map) and E = T - I (step increment).  One theta's
+// table is staged into shared memory with a TMA bulk copy
+// (cp.async.bulk + mbarrier) when it is 16-byte aligned and a multiple of 16
+// bytes, else with plain loads.  Every mbarrier wait is bounded; on timeout
+// the kernel raises a bit in the device error word and stops.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cpab {
+
+constexpr int kMaxDim = 3;
+
+// Bits of the device error word (read back by cpab_device_status()).
+enum : unsigned {
+    kErrTmaTimeout = 1u << 0,   // a bulk copy into shared memory did not complete
+    kErrBadCell = 1u << 1,      // a cell index fell outside [0, nC)
+    kErrScratch = 1u << 2,      // a kernel's scratch region was too small
+};
+
+// Host-computed description of one tessellation.  The float constants are
+// computed exactly as the reference computes them (float inc = 1.0/nc, float
+// products nc*inc) so the FP64 replica below reproduces its comparisons.
+struct Tess {
+    int ndim;
+    int nc[3];
+    int nC;
+    float inc[3];     // (float)(1.0 / nc)
+    float rinc[3];    // (float)(1.0 / inc)  (approximate reciprocal, fast path only)
+    float wlim[3];    // (float)nc * inc     (float product)
+    float clamp3[3];  // 3D clamp limits (float)(nc*inc - 1e-8), z uses inc_x
+    float lim3[3];    // min(clamp3, 1.0f): fast-path upper bound in 3D
+    float eps;        // certified margin of the FP32 fast path
+};
+
+__device__ __forceinline__ int mymin_ref(int a, double b) { return !(b < a) ? a : (int)round(b); }
+
+// ------------------------------- 1D ---------------------------------------
+// Exact in FP32: floor(p * nc) with the float product, clamped
+// (cpab_ops.cu:14-19).
+__device__ __forceinline__ int cell_1d(float p, const Tess &t) {
+    float q = floorf(__fmul_rn(p, (float)t.nc[0]));
+    int idx = (int)q;
+    idx = max(0, min(idx, t.nc[0] - 1));
+    return idx;
+}
+
+// ------------------------------- 2D ---------------------------------------
+// FP64 replica of the reference's 2D lookup (cpab_ops.cpp:33-104).
+static __device__ __noinline__ int cell_2d_exact(float fpx, float fpy, const Tess &t) {
+    const int nx = t.nc[0], ny = t.nc[1];
+    const double px = fpx, py = fpy;
+    const double ix = t.inc[0], iy = t.inc[1];
+    const double wx = t.wlim[0], wy = t.wlim[1];
+    double cx = (0.0 < px) ? px : 0.0;
+    double cy = (0.0 < py) ? py : 0.0;
+    const double mx = wx - 0.000000001, my = wy - 0.000000001;
+    if (cx > mx) cx = mx;
+    if (cy > my) cy = my;
+    const double rx = fmod(cx, ix), ry = fmod(cy, iy);
+    const double fx = rx / ix, fy = ry / iy;
+    int c = 4 * (mymin_ref(nx - 1, (cx - rx) / ix) + mymin_ref(ny - 1, (cy - ry) / iy) * nx);
+    if (px <= 0) {
+        if (py <= 0 && py / iy < px / ix) return c;
+        if (py >= wy && py / iy - ny > -px / ix) return c + 2;
+        return c + 3;
+    }
+    if (px >= wx) {
+        if (py <= 0 && -py / iy > px / ix - nx) return c;
+        if (py >= wy && py / iy - ny > px / ix - nx) return c + 2;
+        return c + 1;
+    }
+    if (py <= 0) return c;
+    if (py >= wy) return c + 2;
+    if (fx < fy) return (1 - fx < fy) ? c + 2 : c + 3;
+    return (1 - fx < fy) ? c + 1 : c;
+}
+
+// Certified FP32 lookup; falls back to the replica when not certain.
+__device__ __forceinline__ int cell_2d(float px, float py, const Tess &t,
+                                       unsigned long long *ties) {
+    const float eps = t.eps;
+    if (px > 0.f && px < t.wlim[0] && py > 0.f && py < t.wlim[1]) {
+        const float qx = px * t.rinc[0], qy = py * t.rinc[1];
+        const float gx = floorf(qx), gy = floorf(qy);
+        const float fx = qx - gx, fy = qy - gy;
+        const float dxy = fx - fy, sxy = (fx + fy) - 1.f;
+        const bool ok = (fx > eps) & (fx < 1.f - eps) & (fy > eps) & (fy < 1.f - eps) &
+                        (fabsf(dxy) > eps) & (fabsf(sxy) > eps);
+        if (ok) {
+            const int c = 4 * ((int)gx + (int)gy * t.nc[0]);
+            return c + (dxy < 0.f ? (sxy > 0.f ? 2 : 3) : (sxy > 0.f ? 1 : 0));
+        }
+    }
+    if (ties) atomicAdd(ties, 1ull);
+    return cell_2d_exact(px, py, t);
+}
+
+// ------------------------------- 3D ---------------------------------------
+// FP64 replica of the reference's 3D lookup (cpab_ops.cpp:106-184), including
+// the push-inside rule that tests only x and y, and the z clamp that uses
+// inc_x.
+static __device__ __noinline__ int cell_3d_exact(float p0, float p1, float p2, const Tess &t) {
+    const int nx = t.nc[0], ny = t.nc[1], nz = t.nc[2];
+    const float ix = t.inc[0], iy = t.inc[1], iz = t.inc[2];
+    float q0 = p0, q1 = p1, q2 = p2;
+    if (q0 < 0.0 || q0 > 1.0 || q1 < 0.0 || q1 > 1.0) {
+        const float h = 0.5f;
+        q0 = __fsub_rn(q0, h); q1 = __fsub_rn(q1, h); q2 = __fsub_rn(q2, h);
+        const float a0 = fabsf(q0), a1 = fabsf(q1), a2 = fabsf(q2);
+        const float s0 = (a0 < a1 && a0 < a2) ? __fmul_rn(h, ix) : 0.0f;
+        const float s1 = (a1 < a0 && a0 < a2) ? __fmul_rn(h, iy) : 0.0f;
+        const float s2 = (a2 < a0 && a0 < a1) ? __fmul_rn(h, iz) : 0.0f;
+        if (a0 > h) q0 = copysignf(__fsub_rn(h, s0), q0);
+        if (a1 > h) q1 = copysignf(__fsub_rn(h, s1), q1);
+        if (a2 > h) q2 = copysignf(__fsub_rn(h, s2), q2);
+        q0 = __fadd_rn(q0, h); q1 = __fadd_rn(q1, h); q2 = __fadd_rn(q2, h);
+    }
+    const float zero = 0.0f;
+    float c0 = (zero < q0) ? q0 : zero; if (q0 != q0) c0 = zero;
+    float c1 = (zero < q1) ? q1 : zero; if (q1 != q1) c1 = zero;
+    float c2 = (zero < q2) ? q2 : zero; if (q2 != q2) c2 = zero;
+    if (t.clamp3[0] < c0) c0 = t.clamp3[0];
+    if (t.clamp3[1] < c1) c1 = t.clamp3[1];
+    if (t.clamp3[2] < c2) c2 = t.clamp3[2];
+    const double r0 = fmod((double)c0, (double)ix);
+    const double r1 = fmod((double)c1, (double)iy);
+    const double r2 = fmod((double)c2, (double)iz);
+    const int i = mymin_ref(nx - 1, ((double)c0 - r0) / (double)ix);
+    const int j = mymin_ref(ny - 1, ((double)c1 - r1) / (double)iy);
+    const int k = mymin_ref(nz - 1, ((double)c2 - r2) / (double)iz);
+    int c = 5 * (i + j * nx + k * nx * ny);
+    double x = r0 / (double)ix, y = r1 / (double)iy, z = r2 / (double)iz;
+    bool flip;
+    if (k % 2 == 0) flip = (i % 2 == 0 && j % 2 == 1) || (i % 2 == 1 && j % 2 == 0);
+    else flip = (i % 2 == 0 && j % 2 == 0) || (i % 2 == 1 && j % 2 == 1);
+    if (flip) { const double tmp = x; x = y; y = 1 - tmp; }
+    if (-x - y + z >= 0) return c + 1;
+    if (x + y + z - 2 >= 0) return c + 2;
+    if (-x + y - z >= 0) return c + 3;
+    if (x - y - z >= 0) return c + 4;
+    return c;
+}
+
+__device__ __forceinline__ int cell_3d(float p0, float p1, float p2, const Tess &t,
+                                       unsigned long long *ties) {
+    const float eps = t.eps;
+    if (p0 > 0.f && p0 < t.lim3[0] && p1 > 0.f && p1 < t.lim3[1] && p2 > 0.f &&
+        p2 < t.lim3[2]) {
+        const float q0 = p0 * t.rinc[0], q1 = p1 * t.rinc[1], q2 = p2 * t.rinc[2];
+        const float g0 = floorf(q0), g1 = floorf(q1), g2 = floorf(q2);
+        float x = q0 - g0, y = q1 - g1;
+        const float z = q2 - g2;
+        bool ok = (x > eps) & (x < 1.f - eps) & (y > eps) & (y < 1.f - eps) & (z > eps) &
+                  (z < 1.f - eps);
+        if (ok) {
+            const int i = (int)g0, j = (int)g1, k = (int)g2;
+            const bool flip = ((i ^ j ^ k) & 1) != 0;   // same parity rule as the reference
+            if (flip) { const float tmp = x; x = y; y = 1.f - tmp; }
+            const int c = 5 * (i + j * t.nc[0] + k * t.nc[0] * t.nc[1]);
+            const float t1 = (z - x) - y;
+            if (fabsf(t1) > eps) {
+                if (t1 > 0.f) return c + 1;
+                const float t2 = ((x + y) + z) - 2.f;
+                if (fabsf(t2) > eps) {
+                    if (t2 > 0.f) return c + 2;
+                    const float t3 = (y - x) - z;
+                    if (fabsf(t3) > eps) {
+                        if (t3 > 0.f) return c + 3;
+                        const float t4 = (x - y) - z;
+                        if (fabsf(t4) > eps) return (t4 > 0.f) ? c + 4 : c;
+                    }
+                }
+            }
+        }
+    }
+    if (ties) atomicAdd(ties, 1ull);
+    return cell_3d_exact(p0, p1, p2, t);
+}
+
+template <int N>
+__device__ __forceinline__ int find_cell(const float (&p)[N], const Tess &t,
+                                         unsigned long long *ties) {
+    if constexpr (N == 1) return cell_1d(p[0], t);
+    else if constexpr (N == 2) return cell_2d(p[0], p[1], t, ties);
+    else return cell_3d(p[0], p[1], p[2], t, ties);
+}
+
+// --------------------------- device error word ------------------------------
+__device__ __forceinline__ void raise_error(unsigned *err, unsigned bits) {
+    if (err) atomicOr(err, bits);
+}
+
+// --------------------------- TMA bulk staging -------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: each try_wait suspends for a hardware time slice, so the
+// limit corresponds to well over a second before giving up.
+constexpr unsigned kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity) {
+    for (unsigned it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// Copy `floats` floats from global src to shared dst.  Collective over the
+// CTA; must be called by all threads.  Returns false (after raising
+// kErrTmaTimeout) if the bulk copy did not complete in time; the caller must
+// then return without touching dst.
+__device__ __forceinline__ bool stage_table(float *dst, const float *src, int floats,
+                                            uint64_t *bar, unsigned *err) {
+    const unsigned bytes = (unsigned)floats * 4u;
+    const bool use_tma = ((reinterpret_cast<uintptr_t>(src) & 15u) == 0) && ((bytes & 15u) == 0) &&
+                         bytes > 0;
+    if (!use_tma) {
+        for (int i = threadIdx.x; i < floats; i += blockDim.x) dst[i] = __ldg(src + i);
+        __syncthreads();
+        return true;
+    }
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(bar, bytes);
+        constexpr unsigned kChunk = 16384;
+        for (unsigned off = 0; off < bytes; off += kChunk) {
+            const unsigned n = (bytes - off < kChunk) ? (bytes - off) : kChunk;
+            bulk_g2s(reinterpret_cast<char *>(dst) + off, reinterpret_cast<const char *>(src) + off,
+                     n, bar);
+        }
+    }
+    bool ok = mbar_wait_bounded(bar, 0);
+    if (!ok) {
+        raise_error(err, kErrTmaTimeout);
+        mbar_wait_bounded(bar, 0);   // give copies in flight a second bounded chance
+    }
+    ok = __syncthreads_and(ok);
+    return ok;
+}
+
+// ---------------------------- affine helpers ---------------------------------
+// y = M[:, :N] x + M[:, N] for one cell map (row-major N x (N+1)).
+template <int N>
+__device__ __forceinline__ void affine_apply(const float *M, const float (&x)[N], float (&y)[N]) {
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+        float acc = M[r * (N + 1) + N];
+#pragma unroll
+        for (int c = 0; c < N; ++c) acc = fmaf(M[r * (N + 1) + c], x[c], acc);
+        y[r] = acc;
+    }
+}
+
+// Load one cell's N x (N+1) map from shared memory into registers.
+template <int N>
+__device__ __forceinline__ void load_cell(const float *tab, int c, float (&M)[N * (N + 1)]) {
+    const float *src = tab + c * (N * (N + 1));
+    if constexpr (N == 1) {
+        const float2 v = *reinterpret_cast<const float2 *>(src);
+        M[0] = v.x; M[1] = v.y;
+    } else if constexpr (N == 2) {
+        const float2 a = reinterpret_cast<const float2 *>(src)[0];
+        const float2 b = reinterpret_cast<const float2 *>(src)[1];
+        const float2 d = reinterpret_cast<const float2 *>(src)[2];
+        M[0] = a.x; M[1] = a.y; M[2] = b.x; M[3] = b.y; M[4] = d.x; M[5] = d.y;
+    } else {
+        const float4 a = reinterpret_cast<const float4 *>(src)[0];
+        const float4 b = reinterpret_cast<const float4 *>(src)[1];
+        const float4 d = reinterpret_cast<const float4 *>(src)[2];
+        M[0] = a.x; M[1] = a.y; M[2] = a.z; M[3] = a.w;
+        M[4] = b.x; M[5] = b.y; M[6] = b.z; M[7] = b.w;
+        M[8] = d.x; M[9] = d.y; M[10] = d.z; M[11] = d.w;
+    }
+}
+
+}  // namespace cpab

@@ -1,0 +1,300 @@
+// Fused transform_data: meshgrid -> integrate -> sample, and its backward.
+//
+// The reference's transform_data (libcpab/cpab.py:304-331) is
+// uniform_meshgrid -> transform_grid -> interpolate: the transformed grid
+// round-trips through global memory between two separate launches (and the
+// interpolation itself is ~30 PyTorch launches).  Here one kernel builds each
+// grid point from the per-axis meshgrid coordinates (the same torch.linspace
+// values the reference uses), integrates it with exactly the arithmetic of
+// k_integrate (compensated update), and samples every channel in registers.
+// Threads are laid out in output order (last axis fastest), so the output
+// writes are coalesced and neighbouring threads read neighbouring pixels.
+//
+// Backward: one kernel per (image, point) that (1) obtains the final position
+// p_N (recomputed along the logged forward pass in "exact" mode, or read back
+// from the forward's saved grid in "reference" mode, whose sensitivity is
+// taken along the midpoint trajectory), (2) applies the interpolation adjoint
+// (scatter into d(data), dL/dp_N through the lerp weights) and (3) runs the
+// trajectory adjoint of cpab_adjoint.cuh, emitting per-CTA partial cell
+// gradients that launch_finalize contracts with the basis.
+#include "cpab_adjoint.cuh"
+#include "cpab_interp.cuh"
+
+namespace cpab {
+
+// Axis indices of output element o (last axis fastest) and its grid point.
+template <int N>
+__device__ __forceinline__ void grid_point(long long o, const Geo &g, const float *lin,
+                                           float (&p)[N]) {
+    long long idx[N];
+    long long r = o;
+#pragma unroll
+    for (int j = N - 1; j >= 0; --j) {
+        idx[j] = r % g.outsize[j];
+        r /= g.outsize[j];
+    }
+    int off = 0;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        p[j] = __ldg(lin + off + idx[j]);
+        off += g.outsize[j];
+    }
+}
+
+template <int N, int PPT>
+__global__ void __launch_bounds__(256)
+    k_transform_data(Tess t, int nsteps, Geo g, const float *__restrict__ lin,
+                     const float *__restrict__ E, int C, const float *__restrict__ data,
+                     float *__restrict__ out, float *__restrict__ grid_out, int tiles,
+                     unsigned long long *ties, unsigned *err) {
+    constexpr int P = N * (N + 1);
+    extern __shared__ float4 smem4[];
+    __shared__ uint64_t bar;
+    float *tab = reinterpret_cast<float *>(smem4);
+    const int b = blockIdx.x / tiles, tile = blockIdx.x % tiles;
+    const int G = t.nC * P;
+    if (!stage_table(tab, E + (long long)b * G, G, &bar, err)) return;
+    float p[PPT][N];
+    long long o[PPT];
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        o[j] = ((long long)tile * PPT + j) * blockDim.x + threadIdx.x;
+        if (o[j] < g.nP) grid_point<N>(o[j], g, lin, p[j]);
+        else {
+#pragma unroll
+            for (int r = 0; r < N; ++r) p[j][r] = 0.5f;
+        }
+    }
+    for (int s = 0; s < nsteps; ++s) {
+#pragma unroll
+        for (int j = 0; j < PPT; ++j) {
+            int c = find_cell<N>(p[j], t, ties);
+            if ((unsigned)c >= (unsigned)t.nC) {
+                raise_error(err, kErrBadCell);
+                c = 0;
+            }
+            float M[P], y[N];
+            load_cell<N>(tab, c, M);
+            affine_apply<N>(M, p[j], y);
+#pragma unroll
+            for (int r = 0; r < N; ++r) p[j][r] += y[r];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        if (o[j] >= g.nP) continue;
+        const Corner<N> cr = corners<N>(p[j], g);
+        for (int c = 0; c < C; ++c)
+            out[((long long)b * C + c) * g.nP + o[j]] =
+                lerp_corners<N>(data + ((long long)b * C + c) * g.nD, cr);
+        if (grid_out) {
+#pragma unroll
+            for (int r = 0; r < N; ++r) grid_out[((long long)b * N + r) * g.nP + o[j]] = p[j][r];
+        }
+    }
+}
+
+cudaError_t launch_transform_data(const Tess &t, int nsteps, const float *lin, const int *outsize,
+                                  const float *E, int nb, const float *data, int C,
+                                  const int *size, float *out, float *grid_out,
+                                  unsigned long long *ties, unsigned *err, cudaStream_t s) {
+    const Geo g = make_geo(t.ndim, size, outsize);
+    if ((long long)nb * g.nP == 0) return cudaSuccess;
+    const int block = 256;
+    const bool two = (long long)nb * g.nP >= (long long)num_sms() * 2048 * 2;
+    const int ppt = two ? 2 : 1;
+    const long long per = (long long)block * ppt;
+    const int tiles = (int)((g.nP + per - 1) / per);
+    const long long grid = (long long)tiles * nb;
+    if (grid > 0x7fffffffll) return cudaErrorInvalidConfiguration;
+    const size_t smem = (size_t)t.nC * t.ndim * (t.ndim + 1) * sizeof(float);
+#define CPAB_TD(N, PP)                                                                         \
+    {                                                                                          \
+        auto kern = k_transform_data<N, PP>;                                                   \
+        if (smem > 48 * 1024) {                                                                \
+            cudaError_t e = cudaFuncSetAttribute(                                              \
+                kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                 \
+            if (e != cudaSuccess) return e;                                                    \
+        }                                                                                      \
+        kern<<<(unsigned)grid, block, smem, s>>>(t, nsteps, g, lin, E, C, data, out, grid_out, \
+                                                 tiles, ties, err);                            \
+        return cudaGetLastError();                                                             \
+    }
+    switch (t.ndim) {
+        case 1: if (two) CPAB_TD(1, 2) else CPAB_TD(1, 1)
+        case 2: if (two) CPAB_TD(2, 2) else CPAB_TD(2, 1)
+        default: if (two) CPAB_TD(3, 2) else CPAB_TD(3, 1)
+    }
+#undef CPAB_TD
+}
+
+template <int N, int MODE, typename CT>
+__global__ void __launch_bounds__(256)
+    k_transform_data_backward(Tess t, int nsteps, Steps st, Geo g, const float *__restrict__ lin,
+                              const float *__restrict__ table,
+                              const float *__restrict__ grid_saved, int C,
+                              const float *__restrict__ data, const float *__restrict__ gout,
+                              float *__restrict__ ddata, float *__restrict__ partials, int parts,
+                              int tiles, unsigned long long *ties, unsigned *err) {
+    constexpr int P = N * (N + 1);
+    extern __shared__ float4 smem4[];
+    __shared__ uint64_t bar;
+    const int B = blockDim.x, tid = threadIdx.x, W = B / 32;
+    const int G = t.nC * P, Gr = round4(G);
+    const int nseg = (nsteps + kSeg - 1) / kSeg;
+    float *tab = reinterpret_cast<float *>(smem4);
+    float *gw = tab + Gr;
+    float *ck = gw + (size_t)W * Gr;
+    CT *cl = reinterpret_cast<CT *>(ck + (size_t)nseg * N * B);
+
+    const int b = blockIdx.x / parts, part = blockIdx.x % parts;
+    if (!stage_table(tab, table + (long long)b * G, G, &bar, err)) return;
+    for (int i = tid; i < W * Gr; i += B) gw[i] = 0.f;
+    __syncthreads();
+    float *warp_tab = gw + (size_t)(tid >> 5) * Gr;
+
+    for (int tile = part; tile < tiles; tile += parts) {
+        const long long o = (long long)tile * B + tid;
+        const bool live = o < g.nP;
+        float p[N], pN[N], lam[N];
+        if (live) grid_point<N>(o, g, lin, p);
+        else {
+#pragma unroll
+            for (int r = 0; r < N; ++r) p[r] = 0.5f;
+        }
+        logged_forward<N, MODE, CT>(tab, t, nsteps, st, p, ck, cl, ties, err);
+#pragma unroll
+        for (int r = 0; r < N; ++r) {
+            if constexpr (MODE == 1) pN[r] = p[r];
+            else pN[r] = live ? __ldg(grid_saved + ((long long)b * N + r) * g.nP + o) : 0.5f;
+        }
+        float gf[N];
+#pragma unroll
+        for (int r = 0; r < N; ++r) gf[r] = 0.f;
+        if (live) {
+            const Corner<N> cr = corners<N>(pN, g);
+            for (int c = 0; c < C; ++c) {
+                const long long plane = ((long long)b * C + c);
+                const float w = __ldg(gout + plane * g.nP + o);
+                lerp_grads<N>(data + plane * g.nD, cr, w, ddata ? ddata + plane * g.nD : nullptr,
+                              gf);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < N; ++r) lam[r] = gf[r] * (float)(g.size[r] - 1);
+        reverse_sweep<N, MODE, CT>(tab, ck, cl, nsteps, st, live, lam, warp_tab);
+    }
+    __syncthreads();
+    float *dst = partials + ((long long)b * parts + part) * G;
+    for (int i = tid; i < G; i += B) {
+        float s = 0.f;
+        for (int w = 0; w < W; ++w) s += gw[(size_t)w * Gr + i];
+        dst[i] = s;
+    }
+}
+
+template <int N, int MODE, typename CT>
+static bool plan_td_t(const Tess &t, int nsteps, long long nP, int nb, AdjointPlan *plan) {
+    int dev = 0, max_optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (max_optin <= 0) max_optin = 48 * 1024;
+    const int cands[3] = {256, 128, 64};
+    for (int ci = 0; ci < 3; ++ci) {
+        const int block = cands[ci];
+        const size_t smem = adjoint_smem_bytes<N, CT>(t.nC, nsteps, block) + 64;
+        if (smem > (size_t)max_optin) continue;
+        auto kern = k_transform_data_backward<N, MODE, CT>;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return false;
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
+        if (per_sm <= 0) continue;
+        const long long tiles = (nP + block - 1) / block;
+        const long long target = 2ll * num_sms() * per_sm;
+        long long parts = (target + nb - 1) / nb;
+        if (parts > tiles) parts = tiles;
+        if (parts < 1) parts = 1;
+        plan->block = block;
+        plan->tiles = (int)tiles;
+        plan->parts = (int)parts;
+        plan->smem = smem;
+        plan->partial_floats = (size_t)nb * parts * t.nC * N * (N + 1);
+        return true;
+    }
+    return false;
+}
+
+bool plan_transform_data_backward(const Tess &t, int nsteps, int mode, long long nP, int nb,
+                                  AdjointPlan *plan) {
+    const bool small = t.nC <= 256;
+#define CPAB_PLAN(N)                                                                          \
+    if (mode == 0)                                                                            \
+        return small ? plan_td_t<N, 0, uint8_t>(t, nsteps, nP, nb, plan)                      \
+                     : plan_td_t<N, 0, uint16_t>(t, nsteps, nP, nb, plan);                    \
+    return small ? plan_td_t<N, 1, uint8_t>(t, nsteps, nP, nb, plan)                          \
+                 : plan_td_t<N, 1, uint16_t>(t, nsteps, nP, nb, plan);
+    switch (t.ndim) {
+        case 1: { CPAB_PLAN(1) }
+        case 2: { CPAB_PLAN(2) }
+        default: { CPAB_PLAN(3) }
+    }
+#undef CPAB_PLAN
+}
+
+template <int N, int MODE, typename CT>
+static cudaError_t launch_td_bwd_t(const Tess &t, int nsteps, const AdjointPlan &plan,
+                                   const Geo &g, const float *lin, const float *table,
+                                   const float *grid_saved, int nb, const float *data, int C,
+                                   const float *gout, float *ddata, float *partials,
+                                   unsigned long long *ties, unsigned *err, cudaStream_t s) {
+    auto kern = k_transform_data_backward<N, MODE, CT>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)plan.smem);
+    if (e != cudaSuccess) return e;
+    Steps st;
+    st.h = (float)(1.0 / nsteps);
+    st.hh = (float)(0.5 / nsteps);
+    st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
+    const long long grid = (long long)nb * plan.parts;
+    if (grid == 0) return cudaSuccess;
+    kern<<<(unsigned)grid, plan.block, plan.smem, s>>>(t, nsteps, st, g, lin, table, grid_saved, C,
+                                                       data, gout, ddata, partials, plan.parts,
+                                                       plan.tiles, ties, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transform_data_backward(const Tess &t, int nsteps, int mode,
+                                           const AdjointPlan &plan, const float *lin,
+                                           const int *outsize, const float *table,
+                                           const float *grid_saved, int nb, const float *data,
+                                           int C, const int *size, const float *gout,
+                                           float *ddata, float *partials,
+                                           unsigned long long *ties, unsigned *err,
+                                           cudaStream_t s) {
+    const Geo g = make_geo(t.ndim, size, outsize);
+    const bool small = t.nC <= 256;
+#define CPAB_TDB(N)                                                                             \
+    if (mode == 0)                                                                              \
+        return small ? launch_td_bwd_t<N, 0, uint8_t>(t, nsteps, plan, g, lin, table,           \
+                                                      grid_saved, nb, data, C, gout, ddata,     \
+                                                      partials, ties, err, s)                   \
+                     : launch_td_bwd_t<N, 0, uint16_t>(t, nsteps, plan, g, lin, table,          \
+                                                       grid_saved, nb, data, C, gout, ddata,    \
+                                                       partials, ties, err, s);                 \
+    return small ? launch_td_bwd_t<N, 1, uint8_t>(t, nsteps, plan, g, lin, table, grid_saved,   \
+                                                  nb, data, C, gout, ddata, partials, ties,     \
+                                                  err, s)                                       \
+                 : launch_td_bwd_t<N, 1, uint16_t>(t, nsteps, plan, g, lin, table, grid_saved,  \
+                                                   nb, data, C, gout, ddata, partials, ties,    \
+                                                   err, s);
+    switch (t.ndim) {
+        case 1: { CPAB_TDB(1) }
+        case 2: { CPAB_TDB(2) }
+        default: { CPAB_TDB(3) }
+    }
+#undef CPAB_TDB
+}
+
+}  // namespace cpab

@@ -1,0 +1,151 @@
+// Forward integration of points through the CPA field (transform_grid).
+//
+// Same scheme as the reference kernels (libcpab/core/cpab_ops.cu:268-388): for
+// nsteps steps, look up the cell of p and apply that cell's step map.  Design
+// on sm_103a:
+//   * one CTA per (theta, tile of blockDim*PPT points); the theta's cell table
+//     is staged in shared memory once by a TMA bulk copy (the reference
+//     re-reads T_c from global memory at every step);
+//   * each thread integrates PPT independent points interleaved, so the
+//     dependent lookup -> load -> affine chain of one trajectory overlaps with
+//     the others';
+//   * certified FP32 cell lookup (cpab_common.cuh) instead of the reference's
+//     FP64 fmod/divide at every step;
+//   * compensated update p <- p + E [p;1] with E = T - I (or the reference's
+//     p <- T [p;1] when handed the reference's T tables);
+//   * structure-of-arrays point I/O, coalesced along the point index.
+#include "cpab_launch.h"
+
+namespace cpab {
+
+template <int N, bool COMP, int PPT>
+__global__ void __launch_bounds__(256)
+    k_integrate(Tess t, int nsteps, const float *__restrict__ points, int broadcast, long long nP,
+                const float *__restrict__ table, int tiles, float *__restrict__ out,
+                unsigned long long *ties, unsigned *err) {
+    constexpr int P = N * (N + 1);
+    extern __shared__ float4 smem4[];
+    __shared__ uint64_t bar;
+    float *tab = reinterpret_cast<float *>(smem4);
+    const int th = blockIdx.x / tiles;
+    const int tile = blockIdx.x % tiles;
+    const int tab_floats = t.nC * P;
+    if (!stage_table(tab, table + (long long)th * tab_floats, tab_floats, &bar, err)) return;
+
+    const float *src = points + (broadcast ? (long long)th * N * nP : 0ll);
+    float p[PPT][N];
+    long long idx[PPT];
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        idx[j] = ((long long)tile * PPT + j) * blockDim.x + threadIdx.x;
+        const bool v = idx[j] < nP;
+#pragma unroll
+        for (int r = 0; r < N; ++r) p[j][r] = v ? __ldg(src + r * nP + idx[j]) : 0.5f;
+    }
+    for (int s = 0; s < nsteps; ++s) {
+#pragma unroll
+        for (int j = 0; j < PPT; ++j) {
+            int c = find_cell<N>(p[j], t, ties);
+            if ((unsigned)c >= (unsigned)t.nC) {   // cannot happen for finite input
+                raise_error(err, kErrBadCell);
+                c = 0;
+            }
+            float M[P], y[N];
+            load_cell<N>(tab, c, M);
+            affine_apply<N>(M, p[j], y);
+#pragma unroll
+            for (int r = 0; r < N; ++r) p[j][r] = COMP ? p[j][r] + y[r] : y[r];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < PPT; ++j) {
+        if (idx[j] < nP) {
+#pragma unroll
+            for (int r = 0; r < N; ++r) out[((long long)th * N + r) * nP + idx[j]] = p[j][r];
+        }
+    }
+}
+
+template <int N, bool COMP, int PPT>
+static cudaError_t launch_integrate_t(const Tess &t, int nsteps, const float *points,
+                                      int broadcast, long long nP, const float *table,
+                                      int n_theta, float *out, unsigned long long *ties,
+                                      unsigned *err, cudaStream_t s) {
+    constexpr int block = 256;
+    const long long per = (long long)block * PPT;
+    const int tiles = (int)((nP + per - 1) / per);
+    const long long grid = (long long)tiles * n_theta;
+    if (grid == 0) return cudaSuccess;
+    if (grid > 0x7fffffffll) return cudaErrorInvalidConfiguration;
+    const size_t smem = (size_t)t.nC * N * (N + 1) * sizeof(float);
+    auto kern = k_integrate<N, COMP, PPT>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    kern<<<(unsigned)grid, block, smem, s>>>(t, nsteps, points, broadcast, nP, table, tiles, out,
+                                             ties, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_integrate(const Tess &t, int nsteps, const float *points, int broadcast,
+                             long long nP, const float *table, bool compensated, int n_theta,
+                             float *out, unsigned long long *ties, unsigned *err,
+                             cudaStream_t s) {
+    // Two points per thread once there is enough work to fill the GPU twice.
+    const bool two = (long long)n_theta * nP >= (long long)num_sms() * 2048 * 2;
+#define CPAB_INTEGRATE(N)                                                                        \
+    if (compensated)                                                                             \
+        return two ? launch_integrate_t<N, true, 2>(t, nsteps, points, broadcast, nP, table,    \
+                                                    n_theta, out, ties, err, s)                  \
+                   : launch_integrate_t<N, true, 1>(t, nsteps, points, broadcast, nP, table,    \
+                                                    n_theta, out, ties, err, s);                 \
+    return two ? launch_integrate_t<N, false, 2>(t, nsteps, points, broadcast, nP, table,       \
+                                                 n_theta, out, ties, err, s)                     \
+               : launch_integrate_t<N, false, 1>(t, nsteps, points, broadcast, nP, table,       \
+                                                 n_theta, out, ties, err, s);
+    switch (t.ndim) {
+        case 1: { CPAB_INTEGRATE(1) }
+        case 2: { CPAB_INTEGRATE(2) }
+        default: { CPAB_INTEGRATE(3) }
+    }
+#undef CPAB_INTEGRATE
+}
+
+template <int N>
+__global__ void k_findcellidx(Tess t, const float *__restrict__ points, long long nP,
+                              int *__restrict__ out, unsigned long long *ties) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nP) return;
+    float p[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) p[r] = points[r * nP + i];
+    out[i] = find_cell<N>(p, t, ties);
+}
+
+cudaError_t launch_findcellidx(const Tess &t, const float *points, long long nP, int *out,
+                               unsigned long long *ties, cudaStream_t s) {
+    if (nP == 0) return cudaSuccess;
+    const int block = 256;
+    const unsigned grid = (unsigned)((nP + block - 1) / block);
+    switch (t.ndim) {
+        case 1: k_findcellidx<1><<<grid, block, 0, s>>>(t, points, nP, out, ties); break;
+        case 2: k_findcellidx<2><<<grid, block, 0, s>>>(t, points, nP, out, ties); break;
+        default: k_findcellidx<3><<<grid, block, 0, s>>>(t, points, nP, out, ties); break;
+    }
+    return cudaGetLastError();
+}
+
+int num_sms() {
+    static int cached = 0;
+    if (cached == 0) {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cached = n > 0 ? n : 148;
+    }
+    return cached;
+}
+
+}  // namespace cpab

@@ -1,0 +1,90 @@
+// Internal launch interface between the C-ABI layer (cpab_capi.cu) and the
+// kernel translation units.  Not part of the public ABI (see include/).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "cpab_common.cuh"
+
+namespace cpab {
+
+// Per-(theta, cell) tables from theta and the basis B [D, d] (fp32):
+// A = B theta, T = expm(dt [A;0]) (rows 0..ndim-1), E = T - I.
+cudaError_t launch_cell_tables(const Tess &t, int nsteps, const float *theta, int n_theta, int d,
+                               const float *basis, float *A, float *T, float *E,
+                               cudaStream_t s);
+
+// Forward integration.  `table` holds T (compensated=false, p <- T p~) or
+// E (compensated=true, p <- p + E p~).
+cudaError_t launch_integrate(const Tess &t, int nsteps, const float *points, int broadcast,
+                             long long nP, const float *table, bool compensated, int n_theta,
+                             float *out, unsigned long long *ties, unsigned *err,
+                             cudaStream_t s);
+
+cudaError_t launch_findcellidx(const Tess &t, const float *points, long long nP, int *out,
+                               unsigned long long *ties, cudaStream_t s);
+
+// Adjoint (backward) of the integration.
+//   mode 0: transpose of the reference's midpoint-rule sensitivity
+//           (table = A);
+//   mode 1: exact discrete adjoint of p <- p + E p~ (table = E).
+// Writes per-CTA partial cell gradients to `partials`
+// ([n_theta, parts, nC*ndim*(ndim+1)] floats) and optionally dL/dpoints
+// per theta ([n_theta, ndim, nP]).
+struct AdjointPlan {
+    int block;           // threads per CTA
+    int parts;           // CTAs per theta
+    int tiles;           // point tiles per theta
+    size_t smem;         // dynamic shared memory bytes
+    size_t partial_floats;
+};
+bool plan_adjoint(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan);
+bool plan_adjoint_mode(const Tess &t, int nsteps, int mode, long long nP, int n_theta,
+                       AdjointPlan *plan);
+cudaError_t launch_adjoint(const Tess &t, int nsteps, int mode, const AdjointPlan &plan,
+                           const float *points, int broadcast, long long nP, const float *table,
+                           int n_theta, const float *gout, float *dpoints, float *partials,
+                           unsigned long long *ties, unsigned *err, cudaStream_t s);
+
+// Sum the partials (fixed order), map cell gradients to dL/dA (mode 1: through
+// the adjoint Frechet derivative of expm), and contract with the basis:
+// dtheta[theta, k] = sum_i B[i, k] dA[i].
+cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *partials, int parts,
+                            const float *A, const float *basis, int d, int n_theta,
+                            float *dtheta, cudaStream_t s);
+
+// Linear / bilinear / trilinear sampling (libcpab/pytorch/interpolation.py).
+cudaError_t launch_interpolate(int ndim, const float *data, int nb, int C, const int *size,
+                               const float *grid, const int *outsize, float *out,
+                               cudaStream_t s);
+cudaError_t launch_interpolate_backward(int ndim, const float *data, int nb, int C,
+                                        const int *size, const float *grid, const int *outsize,
+                                        const float *gout, float *ddata, float *dgrid,
+                                        cudaStream_t s);
+
+// Fused transform_data: meshgrid -> integrate (E) -> sample.  lin holds the
+// per-axis meshgrid coordinates (outsize[0] + outsize[1] + ... floats).
+// grid_out (nullable) receives the transformed grid [nb, ndim, nP].
+cudaError_t launch_transform_data(const Tess &t, int nsteps, const float *lin, const int *outsize,
+                                  const float *E, int nb, const float *data, int C,
+                                  const int *size, float *out, float *grid_out,
+                                  unsigned long long *ties, unsigned *err, cudaStream_t s);
+
+bool plan_transform_data_backward(const Tess &t, int nsteps, int mode, long long nP, int nb,
+                                  AdjointPlan *plan);
+
+// Fused transform_data backward: given dL/dout, produce d(data) (accumulated)
+// and the partial cell gradients for launch_finalize.
+cudaError_t launch_transform_data_backward(const Tess &t, int nsteps, int mode,
+                                           const AdjointPlan &plan, const float *lin,
+                                           const int *outsize, const float *table,
+                                           const float *grid_saved, int nb, const float *data,
+                                           int C, const int *size, const float *gout,
+                                           float *ddata, float *partials,
+                                           unsigned long long *ties, unsigned *err,
+                                           cudaStream_t s);
+
+int num_sms();
+
+}  // namespace cpab

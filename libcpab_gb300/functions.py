@@ -1,0 +1,203 @@
+"""Backend module for the Cpab class: the function set of
+libcpab/pytorch/functions.py:15-129, computed by the sm_103a kernels.
+
+``transformer``, ``interpolate`` and ``findcellidx`` run on CUDA tensors only;
+there is no CPU path.  The small tensor utilities keep the reference's
+semantics so that ``Cpab`` code written against libcpab's pytorch backend
+binds to this module unchanged (libcpab/cpab.py:112-118 selects a backend
+module by name).
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _native as N
+from ._autograd import TransformGrid, TransformGridNumeric, Interpolate, TransformData
+
+
+# ---------------------------------------------------------------- utilities --
+def assert_version():
+    major, minor = (int(x) for x in torch.__version__.split('+')[0].split('.')[:2])
+    assert (major, minor) >= (1, 0), 'PyTorch 1.0 or newer is required'
+
+
+def _device(device):
+    if isinstance(device, str):
+        return torch.device('cuda') if device == 'gpu' else torch.device(device)
+    return device
+
+
+def to(x, dtype=torch.float32, device=None):
+    return torch.tensor(x, dtype=dtype, device=_device(device))
+
+
+def tonumpy(x):
+    return x.detach().cpu().numpy()
+
+
+def check_device(x, device_name):
+    return x.is_cuda == (device_name == 'gpu')
+
+
+def backend_type():
+    return torch.Tensor
+
+
+def pdist(mat):
+    norm = torch.sum(mat * mat, 1).reshape(-1, 1)
+    return norm - 2 * mat.mm(mat.t()) + norm.t()
+
+
+def norm(x):
+    return torch.norm(x)
+
+
+def matmul(x, y):
+    return torch.matmul(x, y)
+
+
+def transpose(x):
+    return x.t()
+
+
+def exp(x):
+    return torch.exp(x)
+
+
+def zeros(*s, device=None):
+    return torch.zeros(*s, device=_device(device))
+
+
+def ones(*s, device=None):
+    return torch.ones(*s, device=_device(device))
+
+
+def arange(x):
+    return torch.arange(x)
+
+
+def repeat(x, reps):
+    return x.repeat(reps)
+
+
+def batch_repeat(x, reps):
+    return x.repeat(reps, *(x.dim() * [1]))
+
+
+def maximum(x):
+    return x.max()
+
+
+def sample_transformation(d, n_sample=1, mean=None, cov=None, device='cpu'):
+    dev = _device(device)
+    mean = torch.zeros(d, dtype=torch.float32, device=dev) if mean is None else mean
+    cov = torch.eye(d, dtype=torch.float32, device=dev) if cov is None else cov
+    dist = torch.distributions.MultivariateNormal(mean, cov)
+    return dist.sample((n_sample,)).to(dev)
+
+
+def identity(d, n_sample=1, epsilon=0, device='cpu'):
+    assert epsilon >= 0, 'epsilon need to be larger than 0'
+    return torch.zeros(n_sample, d, dtype=torch.float32, device=_device(device)) + epsilon
+
+
+def linspaces(domain_min, domain_max, n_points, device):
+    """Per-axis meshgrid coordinates, exactly as uniform_meshgrid builds them."""
+    return [torch.linspace(domain_min[i], domain_max[i], n_points[i], device=_device(device))
+            for i in range(len(n_points))]
+
+
+def uniform_meshgrid(ndim, domain_min, domain_max, n_points, device='cpu'):
+    """[ndim, prod(n_points)] grid with the first axis varying fastest
+    (libcpab/pytorch/functions.py:102-108)."""
+    lin = linspaces(domain_min, domain_max, n_points[:ndim], device)
+    mesh = torch.meshgrid(*lin[::-1], indexing='ij')
+    return torch.cat([g.reshape(1, -1) for g in mesh[::-1]], dim=0)
+
+
+# ---------------------------------------------------------------- hot path ---
+def basis_on(params, device):
+    """fp32 copy of params.basis on `device`, uploaded once and cached."""
+    cache = params.__dict__.setdefault('_basis_cache', {})
+    key = (str(device), id(params.basis))
+    t = cache.get(key)
+    if t is None:
+        t = torch.as_tensor(params.basis, dtype=torch.float32).to(device).contiguous()
+        cache.clear()
+        cache[key] = t
+    return t
+
+
+def _require_cuda(*tensors):
+    for t in tensors:
+        if not t.is_cuda:
+            raise ValueError('libcpab_gb300 computes on CUDA tensors only (no CPU fallback); '
+                             'got a tensor on %s' % t.device)
+
+
+def transformer(points, theta, params):
+    """Integrate points [ndim, nP] or [n_theta, ndim, nP] through the field of
+    every theta [n_theta, d]; returns [n_theta, ndim, nP]
+    (libcpab/pytorch/transformer.py:72-87, 131-202)."""
+    _require_cuda(points, theta)
+    if points.dim() == 3 and points.shape[0] != theta.shape[0]:
+        raise ValueError('a batched grid needs one grid per theta (%d vs %d)'
+                         % (points.shape[0], theta.shape[0]))
+    if points.shape[-2] != params.ndim:
+        raise ValueError('points must have %d coordinates (got %d)' % (params.ndim, points.shape[-2]))
+    if params.numeric_grad:
+        return TransformGridNumeric.apply(points, theta, params)
+    return TransformGrid.apply(points, theta, params)
+
+
+def interpolate(ndim, data, grid, outsize):
+    """Sample data [n_b, C, *size] at grid [n_b, ndim, prod(outsize)]
+    (libcpab/pytorch/interpolation.py:12-172)."""
+    _require_cuda(data, grid)
+    outsize = [int(o) for o in outsize]
+    if data.dim() != ndim + 2:
+        raise ValueError('data must be [n_batch, n_channels, *%dD size]' % ndim)
+    if grid.dim() != 3 or grid.shape[1] != ndim or grid.shape[0] != data.shape[0]:
+        raise ValueError('grid must be [n_batch=%d, %d, n_points]' % (data.shape[0], ndim))
+    n = 1
+    for o in outsize[:ndim]:
+        n *= o
+    if grid.shape[2] != n:
+        raise ValueError('grid has %d points but outsize %s needs %d' % (grid.shape[2], outsize, n))
+    return Interpolate.apply(data, grid, tuple(outsize[:ndim]))
+
+
+def transform_data(data, theta, params, outsize):
+    """Fused uniform_meshgrid -> transformer -> interpolate (libcpab/cpab.py:304-331)."""
+    _require_cuda(data, theta)
+    outsize = tuple(int(o) for o in outsize[:params.ndim])
+    if data.dim() != params.ndim + 2:
+        raise ValueError('data must be [n_batch, n_channels, *%dD size]' % params.ndim)
+    if data.shape[0] != theta.shape[0]:
+        raise ValueError('data and theta must have the same batch size (%d vs %d)'
+                         % (data.shape[0], theta.shape[0]))
+    if params.numeric_grad:
+        grid = uniform_meshgrid(params.ndim, params.domain_min, params.domain_max, outsize,
+                                data.device)
+        return interpolate(params.ndim, data, transformer(grid, theta, params), outsize)
+    return TransformData.apply(data, theta, params, outsize)
+
+
+def findcellidx(ndim, p, nc):
+    """Cell index of each column of p [ndim, nP] (int64), with the reference's
+    C++/CUDA lookup rules (libcpab/core/cpab_ops.cpp:26-190)."""
+    _require_cuda(p)
+    pts = p.detach().to(torch.float32).contiguous()
+    return N.findcellidx(list(nc)[:ndim], pts).to(torch.int64)
+
+
+def calc_vectorfield(grid, theta, params):
+    """Velocity at each point of grid [ndim, nP] for one theta
+    (libcpab/pytorch/functions.py:111-129)."""
+    _require_cuda(grid, theta)
+    B = basis_on(params, theta.device)
+    As = torch.matmul(B, theta.flatten().to(torch.float32)).reshape(params.nC, *params.Ashape)
+    idx = findcellidx(params.ndim, grid, params.nc)
+    gh = torch.cat((grid, torch.ones(1, grid.shape[1], device=grid.device, dtype=grid.dtype)), 0)
+    v = torch.matmul(As[idx], gh.t()[:, :, None])
+    return v[:, :, 0].t()

@@ -1,0 +1,400 @@
+"""CPU oracle for the CPAB integration path.  TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, and only as the checker.  The libcpab_gb300 package never imports it.
+
+Three independent restatements of the reference's algorithm:
+
+* ``Oracle`` -- ctypes front-end of oracle/cpab_oracle.c, a C restatement of
+  libcpab/core/cpab_ops.cpp (cell lookup, fixed-step forward, midpoint-rule
+  sensitivity gradient) and of libcpab/pytorch/interpolation.py.
+* ``numpy_transform_grid`` -- FP64 restatement of the reference's numpy
+  backend (libcpab/numpy/transformer.py:22-61, libcpab/numpy/findcellidx.py),
+  using scipy.linalg.expm per cell.
+* ``fp64_autograd`` -- FP64 torch autograd through the same fixed-step scheme
+  (B theta -> matrix_exp(dT [A;0]) -> gather -> affine, nstepsolver times),
+  with the cell sequence frozen from the FP64 forward pass.  This is the exact
+  derivative of the discrete forward map and the oracle for the exact adjoint.
+
+``RefLib`` loads oracle/_ref/libcpab_ref.so, the reference's own
+libcpab/core/cpab_ops.cpp compiled by oracle/build.py (only where the
+reference checkout exists).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+_f32p = ctypes.POINTER(ctypes.c_float)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_i32p = ctypes.POINTER(ctypes.c_int)
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def n_cells(nc):
+    nc = list(nc)
+    if len(nc) == 1:
+        return nc[0]
+    if len(nc) == 2:
+        return 4 * nc[0] * nc[1]
+    return 5 * nc[0] * nc[1] * nc[2]
+
+
+# --------------------------------------------------------------------------- #
+# C oracle
+# --------------------------------------------------------------------------- #
+class Oracle:
+    def __init__(self, path=None):
+        if path is None:
+            from oracle.build import build_oracle
+            path = build_oracle()
+        self.lib = ctypes.CDLL(path)
+        L = self.lib
+        L.oracle_findcellidx.argtypes = [ctypes.c_int, _i32p, _f32p, ctypes.c_long, _i32p]
+        L.oracle_forward.argtypes = [ctypes.c_int, _i32p, ctypes.c_int, _f32p, ctypes.c_int,
+                                     ctypes.c_long, _f32p, ctypes.c_int, _f32p, _i32p]
+        L.oracle_backward.argtypes = [ctypes.c_int, _i32p, ctypes.c_int, _f32p, ctypes.c_int,
+                                      ctypes.c_long, _f32p, ctypes.c_int, _f32p, ctypes.c_int,
+                                      _f32p, _f64p]
+        L.oracle_interpolate.argtypes = [ctypes.c_int, _f32p, ctypes.c_int, ctypes.c_int, _i32p,
+                                         _f32p, _i32p, _f32p]
+        L.oracle_interpolate_backward.argtypes = [ctypes.c_int, _f32p, ctypes.c_int, ctypes.c_int,
+                                                  _i32p, _f32p, _i32p, _f32p, _f64p, _f32p]
+        L.oracle_num_threads.restype = ctypes.c_int
+        L.oracle_set_threads.argtypes = [ctypes.c_int]
+
+    def num_threads(self):
+        return self.lib.oracle_num_threads()
+
+    def set_threads(self, n):
+        self.lib.oracle_set_threads(int(n))
+
+    def findcellidx(self, nc, points):
+        pts = np.ascontiguousarray(points, dtype=np.float32)
+        ndim, nP = pts.shape
+        nca = np.asarray(nc, dtype=np.int32)
+        out = np.empty(nP, dtype=np.int32)
+        self.lib.oracle_findcellidx(ndim, _p(nca, _i32p), _p(pts, _f32p), nP, _p(out, _i32p))
+        return out
+
+    def forward(self, nc, nsteps, points, trels, return_cells=False):
+        """points [ndim,nP] or [n_theta,ndim,nP]; trels [n_theta,nC,ndim,ndim+1]."""
+        pts = np.ascontiguousarray(points, dtype=np.float32)
+        tr = np.ascontiguousarray(trels, dtype=np.float32)
+        n_theta = tr.shape[0]
+        broadcast = int(pts.ndim == 3 and pts.shape[0] == n_theta)
+        ndim, nP = pts.shape[-2], pts.shape[-1]
+        nca = np.asarray(nc, dtype=np.int32)
+        out = np.empty((n_theta, ndim, nP), dtype=np.float32)
+        cells = np.empty((n_theta, nP, nsteps), dtype=np.int32) if return_cells else None
+        self.lib.oracle_forward(ndim, _p(nca, _i32p), nsteps, _p(pts, _f32p), broadcast, nP,
+                                _p(tr, _f32p), n_theta, _p(out, _f32p),
+                                _p(cells, _i32p) if return_cells else None)
+        return (out, cells) if return_cells else out
+
+    def backward(self, nc, nsteps, points, As, Bs, grad):
+        """Reference analytic dtheta [n_theta, d] (float64 accumulation)."""
+        pts = np.ascontiguousarray(points, dtype=np.float32)
+        A = np.ascontiguousarray(As, dtype=np.float32)
+        B = np.ascontiguousarray(Bs, dtype=np.float32)
+        g = np.ascontiguousarray(grad, dtype=np.float32)
+        n_theta, d = A.shape[0], B.shape[0]
+        broadcast = int(pts.ndim == 3 and pts.shape[0] == n_theta)
+        ndim, nP = pts.shape[-2], pts.shape[-1]
+        nca = np.asarray(nc, dtype=np.int32)
+        out = np.zeros((n_theta, d), dtype=np.float64)
+        self.lib.oracle_backward(ndim, _p(nca, _i32p), nsteps, _p(pts, _f32p), broadcast, nP,
+                                 _p(A, _f32p), n_theta, _p(B, _f32p), d, _p(g, _f32p),
+                                 _p(out, _f64p))
+        return out
+
+    def interpolate(self, data, grid, outsize):
+        D = np.ascontiguousarray(data, dtype=np.float32)
+        G = np.ascontiguousarray(grid, dtype=np.float32)
+        ndim = G.shape[1]
+        nb, C = D.shape[:2]
+        size = np.asarray(D.shape[2:], dtype=np.int32)
+        osz = np.asarray(outsize, dtype=np.int32)
+        out = np.empty((nb, C, *[int(o) for o in outsize]), dtype=np.float32)
+        self.lib.oracle_interpolate(ndim, _p(D, _f32p), nb, C, _p(size, _i32p), _p(G, _f32p),
+                                    _p(osz, _i32p), _p(out, _f32p))
+        return out
+
+    def interpolate_backward(self, data, grid, outsize, gout):
+        D = np.ascontiguousarray(data, dtype=np.float32)
+        G = np.ascontiguousarray(grid, dtype=np.float32)
+        W = np.ascontiguousarray(gout, dtype=np.float32)
+        ndim = G.shape[1]
+        nb, C = D.shape[:2]
+        size = np.asarray(D.shape[2:], dtype=np.int32)
+        osz = np.asarray(outsize, dtype=np.int32)
+        ddata = np.zeros(D.shape, dtype=np.float64)
+        dgrid = np.empty(G.shape, dtype=np.float32)
+        self.lib.oracle_interpolate_backward(ndim, _p(D, _f32p), nb, C, _p(size, _i32p),
+                                             _p(G, _f32p), _p(osz, _i32p), _p(W, _f32p),
+                                             _p(ddata, _f64p), _p(dgrid, _f32p))
+        return ddata, dgrid
+
+
+class RefLib:
+    """The reference's own libcpab/core/cpab_ops.cpp (compiled by oracle/build.py)."""
+
+    def __init__(self, path=None):
+        if path is None:
+            from oracle.build import build_ref
+            path = build_ref()
+        if path is None or not os.path.exists(path):
+            raise FileNotFoundError('reference CPU library not built (no reference checkout)')
+        self.lib = ctypes.CDLL(path)
+        L = self.lib
+        L.ref_findcellidx.argtypes = [ctypes.c_int, _f32p, _i32p]
+        L.ref_findcellidx.restype = ctypes.c_int
+        L.ref_forward.argtypes = [_f32p, _f32p, _f32p, _i32p, _i32p, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_int]
+        L.ref_backward.argtypes = [_f32p, _f32p, _f32p, _f32p, _i32p, _i32p, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int]
+
+    def findcellidx(self, nc, points):
+        pts = np.ascontiguousarray(np.asarray(points, dtype=np.float32).T)
+        nca = np.asarray(nc, dtype=np.int32)
+        return np.array([self.lib.ref_findcellidx(len(nc), _p(pts[i], _f32p), _p(nca, _i32p))
+                         for i in range(pts.shape[0])], dtype=np.int32)
+
+    def forward(self, nc, nsteps, points, trels):
+        pts = np.ascontiguousarray(points, dtype=np.float32)
+        tr = np.ascontiguousarray(trels, dtype=np.float32)
+        n_theta = tr.shape[0]
+        broadcast = int(pts.ndim == 3 and pts.shape[0] == n_theta)
+        ndim, nP = pts.shape[-2], pts.shape[-1]
+        nca = np.asarray(nc, dtype=np.int32)
+        ns = np.asarray([nsteps], dtype=np.int32)
+        out = np.zeros((n_theta, ndim, nP), dtype=np.float32)
+        self.lib.ref_forward(_p(out, _f32p), _p(pts, _f32p), _p(tr, _f32p), _p(ns, _i32p),
+                             _p(nca, _i32p), ndim, nP, n_theta, broadcast)
+        return out
+
+    def backward_sensitivity(self, nc, nsteps, points, As, Bs):
+        """The reference's [d, n_theta, ndim, nP] sensitivity tensor."""
+        pts = np.ascontiguousarray(points, dtype=np.float32)
+        A = np.ascontiguousarray(As, dtype=np.float32)
+        B = np.ascontiguousarray(Bs, dtype=np.float32)
+        n_theta, nC = A.shape[0], A.shape[1]
+        d = B.shape[0]
+        broadcast = int(pts.ndim == 3 and pts.shape[0] == n_theta)
+        ndim, nP = pts.shape[-2], pts.shape[-1]
+        nca = np.asarray(nc, dtype=np.int32)
+        ns = np.asarray([nsteps], dtype=np.int32)
+        out = np.zeros((d, n_theta, ndim, nP), dtype=np.float32)
+        self.lib.ref_backward(_p(out, _f32p), _p(pts, _f32p), _p(A, _f32p), _p(B, _f32p),
+                              _p(ns, _i32p), _p(nca, _i32p), n_theta, d, ndim, nP, nC, broadcast)
+        return out
+
+
+# --------------------------------------------------------------------------- #
+# FP64 numpy restatement of libcpab/numpy (transformer.py:22-61, findcellidx.py)
+# --------------------------------------------------------------------------- #
+def _np_round_min(a, b):
+    return np.where(a < b, a, np.round(b))
+
+
+def numpy_findcellidx(ndim, p, nc):
+    """Vectorised cell lookup with the numpy backend's semantics
+    (libcpab/numpy/findcellidx.py:22-150; in 3D it also tests z when deciding
+    whether a point is outside, unlike the C++/CUDA lookup)."""
+    p = np.array(p, dtype=np.float64, copy=True)
+    if ndim == 1:
+        nx = nc[0]
+        idx = np.floor(p[0] * nx)
+        return np.maximum(0.0, np.minimum(idx, nx - 1)).astype(np.int64)
+    if ndim == 2:
+        nx, ny = nc
+        ix, iy = 1.0 / nx, 1.0 / ny
+        p0 = np.minimum(nx * ix - 1e-8, np.maximum(0.0, p[0]))
+        p1 = np.minimum(ny * iy - 1e-8, np.maximum(0.0, p[1]))
+        xm, ym = np.fmod(p0, ix), np.fmod(p1, iy)
+        x, y = xm / ix, ym / iy
+        idx = _np_round_min(nx - 1, (p0 - xm) / ix) + _np_round_min(ny - 1, (p1 - ym) / iy) * nx
+        idx = idx * 4
+        left = p[0] <= 0
+        c1 = left & (p[1] <= 0) & (p[1] / iy < p[0] / ix)
+        c2 = ~c1 & left & (p[1] >= ny * iy) & (p[1] / iy - ny > -p[0] / ix)
+        c3 = ~c1 & ~c2 & left
+        out = c1 | c2 | c3
+        right = p[0] >= nx * ix
+        c4 = ~out & right & (p[1] <= 0) & (-p[1] / iy > p[0] / ix - nx)
+        c5 = ~out & ~c4 & right & (p[1] >= ny * iy) & (p[1] / iy - ny > p[0] / ix - nx)
+        c6 = ~out & ~c4 & ~c5 & right
+        out = out | c4 | c5 | c6
+        c7 = ~out & (p[1] >= ny * iy)
+        out = out | c7
+        c8 = ~out & (x < y) & (1 - x < y)
+        c9 = ~out & ~c8 & (x < y)
+        c10 = ~out & ~c8 & ~c9 & (x >= y) & (1 - x < y)
+        idx = idx + 2 * (c2 | c5 | c7 | c8) + 3 * (c3 | c9) + 1 * (c6 | c10)
+        return idx.astype(np.int64)
+    nx, ny, nz = nc
+    outside = ((p[0] < 0) | (p[0] > 1) | (p[1] < 0) | (p[1] > 1) | (p[2] < 0) | (p[2] > 1))
+    ix, iy, iz = 1.0 / nx, 1.0 / ny, 1.0 / nz
+    h = 0.5
+    q = p[:, outside] - h
+    a = np.abs(q)
+    push = [(h * ix) * ((a[0] < a[1]) & (a[0] < a[2])),
+            (h * iy) * ((a[1] < a[0]) & (a[0] < a[2])),
+            (h * iz) * ((a[2] < a[0]) & (a[0] < a[1]))]
+    for j in range(3):
+        m = a[j] > h
+        q[j, m] = np.copysign(h - push[j][m], q[j, m])
+    p[:, outside] = q + h
+    p0 = np.minimum(nx * ix - 1e-8, np.maximum(0.0, p[0]))
+    p1 = np.minimum(ny * iy - 1e-8, np.maximum(0.0, p[1]))
+    p2 = np.minimum(nz * iz - 1e-8, np.maximum(0.0, p[2]))
+    xm, ym, zm = np.mod(p0, ix), np.mod(p1, iy), np.mod(p2, iz)
+    i = _np_round_min(nx - 1, (p0 - xm) / ix)
+    j = _np_round_min(ny - 1, (p1 - ym) / iy)
+    k = _np_round_min(nz - 1, (p2 - zm) / iz)
+    idx = 5 * (i + j * nx + k * nx * ny)
+    x, y, z = xm / ix, ym / iy, zm / iz
+    flip = (((k % 2 == 0) & (i % 2 == 0) & (j % 2 == 1)) | ((k % 2 == 0) & (i % 2 == 1) & (j % 2 == 0)) |
+            ((k % 2 == 1) & (i % 2 == 0) & (j % 2 == 0)) | ((k % 2 == 1) & (i % 2 == 1) & (j % 2 == 1)))
+    x, y = np.where(flip, y, x), np.where(flip, 1 - x, y)
+    t1 = -x - y + z >= 0
+    t2 = x + y + z - 2 >= 0
+    t3 = -x + y - z >= 0
+    t4 = x - y - z >= 0
+    idx = idx + 1 * t1 + 2 * (t2 & ~t1) + 3 * (t3 & ~t1 & ~t2) + 4 * (t4 & ~t1 & ~t2 & ~t3)
+    return idx.astype(np.int64)
+
+
+def step_maps_fp64(basis, theta, ndim, nsteps):
+    """T_c = expm(dT [A_c; 0]) in float64, [n_theta, nC, ndim+1, ndim+1]."""
+    from scipy.linalg import expm
+    B = np.asarray(basis, dtype=np.float64)
+    th = np.asarray(theta, dtype=np.float64)
+    n_theta = th.shape[0]
+    nC = B.shape[0] // (ndim * (ndim + 1))
+    A = (B @ th.T).T.reshape(n_theta * nC, ndim, ndim + 1)
+    Asq = np.concatenate([A, np.zeros((n_theta * nC, 1, ndim + 1))], axis=1)
+    dT = 1.0 / nsteps
+    T = np.stack([expm(dT * a) for a in Asq])
+    return T.reshape(n_theta, nC, ndim + 1, ndim + 1)
+
+
+def decision_margin(ndim, p, nc):
+    """Distance (domain units) from each point p [ndim, n] to the nearest
+    boundary that the cell lookup decides on: cell faces, the triangle
+    diagonals (2D), the tetrahedron planes (3D) and the out-of-domain rules.
+    An fp32 trajectory can only take a different cell than the FP64 one at a
+    step whose margin is below its rounding drift (a boundary tie)."""
+    p = np.asarray(p, dtype=np.float64)
+    inc = [1.0 / n for n in nc]
+    m = np.full(p.shape[1], np.inf)
+    for j in range(ndim):
+        q = p[j] / inc[j]
+        m = np.minimum(m, np.abs(q - np.round(q)) * inc[j])
+    if ndim == 1:
+        return m
+    fr = [np.mod(np.clip(p[j], 0, 1 - 1e-12), inc[j]) / inc[j] for j in range(ndim)]
+    if ndim == 2:
+        x, y = fr
+        s = min(inc) / np.sqrt(2)
+        m = np.minimum(m, np.abs(x - y) * s)
+        m = np.minimum(m, np.abs(x + y - 1) * s)
+        # out-of-domain diagonal rules (cpab_ops.cpp:57-79)
+        ox, oy = p[0] / inc[0], p[1] / inc[1]
+        out = (p[0] <= 0) | (p[0] >= 1) | (p[1] <= 0) | (p[1] >= 1)
+        for diff in (oy - ox, oy - nc[1] + ox, -oy - ox + nc[0], oy - nc[1] - ox + nc[0]):
+            m = np.where(out, np.minimum(m, np.abs(diff) * s), m)
+        return m
+    x, y, z = fr
+    s = min(inc) / np.sqrt(3)
+    for xx, yy in ((x, y), (y, 1 - x)):
+        for v in (-xx - yy + z, xx + yy + z - 2, -xx + yy - z, xx - yy - z):
+            m = np.minimum(m, np.abs(v) * s)
+    return m
+
+
+def numpy_transform_grid(basis, theta, points, nc, nsteps=50, return_cells=False,
+                         return_margin=False):
+    """FP64 fixed-step integration with the numpy backend's semantics.
+
+    return_margin adds, per point, the smallest decision_margin met along the
+    trajectory ([n_theta, nP])."""
+    nc = list(nc)
+    ndim = len(nc)
+    th = np.asarray(theta, dtype=np.float64)
+    n_theta = th.shape[0]
+    pts = np.asarray(points, dtype=np.float64)
+    nP = pts.shape[-1]
+    T = step_maps_fp64(basis, th, ndim, nsteps)
+    nC = T.shape[1]
+    P = np.broadcast_to(pts, (n_theta, ndim, nP)) if pts.ndim == 2 else pts
+    P = np.ascontiguousarray(np.transpose(P, (0, 2, 1))).reshape(-1, ndim)
+    Ph = np.concatenate([P, np.ones((P.shape[0], 1))], axis=1)[:, :, None]
+    Tf = T.reshape(n_theta * nC, ndim + 1, ndim + 1)
+    base = np.repeat(np.arange(n_theta) * nC, nP)
+    cells = []
+    margin = np.full(n_theta * nP, np.inf)
+    for _ in range(nsteps):
+        c = numpy_findcellidx(ndim, Ph[:, :ndim, 0].T, nc)
+        if return_margin:
+            margin = np.minimum(margin, decision_margin(ndim, Ph[:, :ndim, 0].T, nc))
+        cells.append(c)
+        Ph = np.matmul(Tf[c + base], Ph)
+    out = Ph[:, :ndim, 0].reshape(n_theta, nP, ndim).transpose(0, 2, 1)
+    res = [out]
+    if return_cells:
+        res.append(np.stack(cells, axis=1).reshape(n_theta, nP, nsteps))
+    if return_margin:
+        res.append(margin.reshape(n_theta, nP))
+    return res[0] if len(res) == 1 else tuple(res)
+
+
+# --------------------------------------------------------------------------- #
+# FP64 autograd oracle for gradients
+# --------------------------------------------------------------------------- #
+def fp64_autograd(basis, theta, points, nc, cotangent, nsteps=50, cells=None):
+    """Exact derivative of the discrete forward map, in float64.
+
+    Returns (out [n_theta,ndim,nP], dtheta [n_theta,d], dpoints like points).
+    The cell at each step is frozen: from ``cells`` ([n_theta,nP,nsteps]) if
+    given, else looked up on the FP64 trajectory with the C++ lookup rules.
+    """
+    import torch
+    nc = list(nc)
+    ndim = len(nc)
+    B = torch.as_tensor(np.asarray(basis, dtype=np.float64))
+    th = torch.tensor(np.asarray(theta, dtype=np.float64), requires_grad=True)
+    pts = torch.tensor(np.asarray(points, dtype=np.float64), requires_grad=True)
+    n_theta = th.shape[0]
+    nC = B.shape[0] // (ndim * (ndim + 1))
+    nP = pts.shape[-1]
+    A = (B @ th.T).T.reshape(n_theta, nC, ndim, ndim + 1)
+    Asq = torch.cat([A, torch.zeros(n_theta, nC, 1, ndim + 1, dtype=A.dtype)], dim=2)
+    T = torch.linalg.matrix_exp(Asq / nsteps)[:, :, :ndim, :]          # [n_theta,nC,n,n+1]
+    P = pts.expand(n_theta, ndim, nP) if pts.dim() == 2 else pts
+    P = P.permute(0, 2, 1)                                               # [n_theta,nP,n]
+    ones = torch.ones(n_theta, nP, 1, dtype=P.dtype)
+    tidx = torch.arange(n_theta)[:, None].expand(n_theta, nP)
+    if cells is None:
+        lookup = Oracle()
+    for s in range(nsteps):
+        if cells is None:
+            pf = P.detach().numpy().reshape(-1, ndim).T.astype(np.float32)
+            c = torch.as_tensor(lookup.findcellidx(nc, pf).astype(np.int64)).reshape(n_theta, nP)
+        else:
+            c = torch.as_tensor(np.asarray(cells)[:, :, s].astype(np.int64))
+        Tc = T[tidx, c]                                                 # [n_theta,nP,n,n+1]
+        Ph = torch.cat([P, ones], dim=2)
+        P = (Tc @ Ph[..., None])[..., 0]
+    out = P.permute(0, 2, 1)
+    w = torch.as_tensor(np.asarray(cotangent, dtype=np.float64))
+    (out * w).sum().backward()
+    return out.detach().numpy(), th.grad.numpy(), pts.grad.numpy()

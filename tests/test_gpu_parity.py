@@ -1,0 +1,252 @@
+"""GPU parity: the sm_103a kernels (through the C ABI) against the reference's
+golden outputs (tests/golden, produced by the reference itself) and against
+the CPU oracle.
+
+Tolerances (written where they are used):
+  * cell lookup: bit-exact;
+  * forward points vs the FP64 oracle of the same scheme: <= 1e-5 of the
+    domain width (max over points);
+  * dtheta vs the reference's analytic gradient (reference mode) and vs the
+    FP64 autograd oracle (exact mode): relative error <= 1e-4, measured as
+    max|diff| / max|ref| per config;
+  * interpolation: <= 1e-6 absolute for values in [0,1], gradients <= 1e-5
+    relative.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import SMALL, load_golden
+
+pytestmark = pytest.mark.gpu
+
+NSTEPS = 50
+
+
+def make_cpab(g, gradient='reference'):
+    from libcpab_gb300 import Cpab
+    nc = [int(x) for x in g['nc']]
+    T = Cpab(nc, backend='pytorch', device='gpu', zero_boundary=bool(g['zero_boundary']),
+             volume_perservation=bool(g['volume_perservation']))
+    # theta only has a meaning relative to the reference's basis: use it
+    T.params.basis = np.asarray(g['B'], dtype=np.float64)
+    T.params.D, T.params.d = T.params.basis.shape
+    T.set_solver_params(nstepsolver=NSTEPS, gradient=gradient)
+    return T
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if b.size == 0:
+        assert a.size == 0
+        return 0.0
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+@pytest.mark.parametrize('name', SMALL)
+def test_findcellidx_bit_exact(name, cuda):
+    from libcpab_gb300 import _native as N
+    g = load_golden(name)
+    nc = [int(x) for x in g['nc']]
+    P = torch.tensor(g['probe'], device=cuda).contiguous()
+    got = N.findcellidx(nc, P).cpu().numpy()
+    ref = g['cells_cpp']
+    bad = np.nonzero(got != ref)[0]
+    assert bad.size == 0, 'cell mismatch at %s: got %s want %s (points %s)' % (
+        bad[:5], got[bad[:5]], ref[bad[:5]], g['probe'][:, bad[:5]].T)
+
+
+@pytest.mark.parametrize('name', SMALL)
+def test_findcellidx_random_vs_oracle(name, cuda, oracle):
+    from libcpab_gb300 import _native as N
+    g = load_golden(name)
+    nc = [int(x) for x in g['nc']]
+    rng = np.random.default_rng(7)
+    P = rng.uniform(-0.3, 1.3, (len(nc), 200000)).astype(np.float32)
+    P[:, :100000] = rng.uniform(0, 1, (len(nc), 100000))
+    got = N.findcellidx(nc, torch.tensor(P, device=cuda)).cpu().numpy()
+    assert np.array_equal(got, oracle.findcellidx(nc, P))
+
+
+@pytest.mark.parametrize('name', SMALL)
+def test_forward_with_reference_step_maps(name, cuda):
+    """cpab_forward fed the reference's own fp32 Pade step maps reproduces the
+    reference's pytorch-CPU result; differences come only from FMA rounding
+    (and from the rare cell choices those roundings flip)."""
+    from libcpab_gb300 import _native as N
+    g = load_golden(name)
+    nc = [int(x) for x in g['nc']]
+    grid = torch.tensor(g['grid'], device=cuda)
+    trels = torch.tensor(g['trels_ref'], device=cuda)
+    out = N.forward_trels(nc, NSTEPS, grid, trels).cpu().numpy()
+    diff = np.abs(out - g['out_cpu32'])
+    assert np.quantile(diff, 0.999) <= 1e-5
+    assert diff.max() <= 1e-3
+
+
+TIE_MARGIN = 1e-6     # trajectories passing closer than this to a decision boundary are ties
+
+
+def check_points_vs_fp64(out, g, grid, ref):
+    """Gate: max point error <= 1e-5 of the domain width on every trajectory
+    that never comes within TIE_MARGIN of a cell-decision boundary; tie-exposed
+    trajectories (the fixed-step scheme is discontinuous there, so fp32 and
+    FP64 may take different cells) are counted, must be rare, and stay
+    bounded."""
+    from oracle.oracle import numpy_transform_grid
+    nc = [int(x) for x in g['nc']]
+    _, margin = numpy_transform_grid(g['B'], g['theta'], grid, nc, NSTEPS, return_margin=True)
+    err = np.abs(out - ref).max(axis=1)                       # [n_theta, nP]
+    exposed = margin < TIE_MARGIN
+    clean = err[~exposed].max() if (~exposed).any() else 0.0
+    assert clean <= 1e-5, 'max error %.3g on tie-free trajectories' % clean
+    assert exposed.mean() <= 0.02, 'tie-exposed fraction %.3g' % exposed.mean()
+    assert err.max() <= 1e-3, 'max error %.3g (tie-exposed)' % err.max()
+    return clean, int(exposed.sum()), float(err.max())
+
+
+@pytest.mark.parametrize('name', SMALL)
+def test_transform_grid_vs_fp64(name, cuda):
+    g = load_golden(name)
+    T = make_cpab(g)
+    th = torch.tensor(g['theta'], device=cuda)
+    out = T.transform_grid(torch.tensor(g['grid'], device=cuda), th).cpu().numpy()
+    check_points_vs_fp64(out, g, g['grid'], g['out_np64'])
+    outb = T.transform_grid(torch.tensor(g['grid_b'], device=cuda), th).cpu().numpy()
+    check_points_vs_fp64(outb, g, g['grid_b'], g['out_np64_b'])
+
+
+@pytest.mark.parametrize('name', SMALL)
+@pytest.mark.parametrize('which', ['grid', 'grid_b'])
+def test_gradient_reference_mode(name, which, cuda):
+    g = load_golden(name)
+    T = make_cpab(g, 'reference')
+    th = torch.tensor(g['theta'], device=cuda, requires_grad=True)
+    out = T.transform_grid(torch.tensor(g[which], device=cuda), th)
+    (out * torch.tensor(g['cot'], device=cuda)).sum().backward()
+    ref = g['dtheta_ref'] if which == 'grid' else g['dtheta_ref_b']
+    r = rel_err(th.grad.cpu().numpy(), ref)
+    assert r <= 1e-4, 'reference-mode dtheta rel err %.3g' % r
+
+
+@pytest.mark.parametrize('name', SMALL)
+def test_gradient_exact_mode(name, cuda):
+    from oracle.oracle import fp64_autograd
+    g = load_golden(name)
+    T = make_cpab(g, 'exact')
+    nc = [int(x) for x in g['nc']]
+    th = torch.tensor(g['theta'], device=cuda, requires_grad=True)
+    pts = torch.tensor(g['grid_b'], device=cuda, requires_grad=True)
+    out = T.transform_grid(pts, th)
+    (out * torch.tensor(g['cot'], device=cuda)).sum().backward()
+    _, dth, dpts = fp64_autograd(g['B'], g['theta'], g['grid_b'], nc, g['cot'], NSTEPS)
+    r = rel_err(th.grad.cpu().numpy(), dth)
+    assert r <= 1e-4, 'exact-mode dtheta rel err %.3g' % r
+    rp = rel_err(pts.grad.cpu().numpy(), dpts)
+    assert rp <= 1e-4, 'exact-mode dpoints rel err %.3g' % rp
+
+
+@pytest.mark.parametrize('name', SMALL)
+def test_backward_deterministic(name, cuda):
+    g = load_golden(name)
+    res = []
+    for mode in ('reference', 'exact'):
+        T = make_cpab(g, mode)
+        outs = []
+        for _ in range(2):
+            th = torch.tensor(g['theta'], device=cuda, requires_grad=True)
+            out = T.transform_grid(torch.tensor(g['grid'], device=cuda), th)
+            (out * torch.tensor(g['cot'], device=cuda)).sum().backward()
+            outs.append(th.grad.cpu().numpy())
+        assert np.array_equal(outs[0], outs[1]), mode
+        res.append(outs[0])
+
+
+@pytest.mark.parametrize('name', SMALL)
+def test_interpolate_vs_reference(name, cuda):
+    g = load_golden(name)
+    T = make_cpab(g)
+    npts = [int(x) for x in g['npts']]
+    data = torch.tensor(g['data'], device=cuda, requires_grad=True)
+    grid = torch.tensor(g['out_cpu32'], device=cuda, requires_grad=True)
+    out = T.interpolate(data, grid, npts)
+    err = np.abs(out.detach().cpu().numpy() - g['interp32']).max()
+    assert err <= 1e-6, 'interpolate max abs err %.3g' % err
+    (out * torch.tensor(g['icot'], device=cuda)).sum().backward()
+    assert rel_err(data.grad.cpu().numpy(), g['interp64_ddata']) <= 1e-5
+    assert rel_err(grid.grad.cpu().numpy(), g['interp64_dgrid']) <= 1e-5
+
+
+@pytest.mark.parametrize('name', SMALL)
+@pytest.mark.parametrize('mode', ['reference', 'exact'])
+def test_transform_data_fused_matches_unfused(name, mode, cuda):
+    """The fused kernel computes exactly transform_grid followed by
+    interpolate; its gradients match the unfused chain."""
+    g = load_golden(name)
+    T = make_cpab(g, mode)
+    osz = [int(x) for x in g['outsize']]
+    th = torch.tensor(g['theta'], device=cuda)
+    data = torch.tensor(g['data'], device=cuda)
+    t1 = th.clone().requires_grad_(True)
+    d1 = data.clone().requires_grad_(True)
+    fused = T.transform_data(d1, t1, osz)
+    t2 = th.clone().requires_grad_(True)
+    d2 = data.clone().requires_grad_(True)
+    grid = T.uniform_meshgrid(osz)
+    unfused = T.interpolate(d2, T.transform_grid(grid, t2), osz)
+    assert torch.equal(fused, unfused)
+    w = torch.randn(fused.shape, device=cuda, generator=torch.Generator(cuda).manual_seed(3))
+    (fused * w).sum().backward()
+    (unfused * w).sum().backward()
+    assert rel_err(d1.grad.cpu().numpy(), d2.grad.cpu().numpy()) <= 1e-5
+    assert rel_err(t1.grad.cpu().numpy(), t2.grad.cpu().numpy()) <= 1e-4
+
+
+@pytest.mark.parametrize('name', SMALL)
+def test_transform_data_vs_reference(name, cuda):
+    """Against the reference's own transform_data and MSE backward.  The
+    reference integrates with fp32 T (error up to ~3e-5 vs FP64), this library
+    with compensated increments, so sampled values differ by the image
+    gradient times that position difference."""
+    g = load_golden(name)
+    T = make_cpab(g, 'reference')
+    osz = [int(x) for x in g['outsize']]
+    th = torch.tensor(g['theta'], device=cuda, requires_grad=True)
+    data = torch.tensor(g['data'], device=cuda, requires_grad=True)
+    out = T.transform_data(data, th, osz)
+    loss = torch.nn.functional.mse_loss(out, torch.tensor(g['td_target'], device=cuda))
+    loss.backward()
+    assert np.abs(out.detach().cpu().numpy() - g['td_out']).max() <= 2e-3
+    assert abs(loss.item() - float(g['td_loss'])) <= 1e-4 * max(abs(float(g['td_loss'])), 1e-6)
+    assert rel_err(th.grad.cpu().numpy(), g['td_dtheta']) <= 2e-3
+    assert rel_err(data.grad.cpu().numpy(), g['td_ddata']) <= 2e-3
+
+
+def test_errors_are_raised(cuda):
+    from libcpab_gb300 import Cpab, _native as N
+    T = Cpab([2, 2], backend='pytorch', device='gpu')
+    th = torch.zeros(2, T.get_theta_dim(), device=cuda)
+    with pytest.raises(AssertionError):
+        T.transform_grid(torch.zeros(2, 10), th)              # CPU grid
+    with pytest.raises(ValueError):
+        T.transform_grid(torch.zeros(3, 2, 10, device=cuda), th.repeat(2, 1)[:1])
+    with pytest.raises(ValueError):
+        T.interpolate(torch.zeros(2, 1, 5, 5, device=cuda), torch.zeros(2, 2, 7, device=cuda),
+                      [3, 3])
+    with pytest.raises(N.CpabError):
+        N.integrate([2, 2], 0, torch.zeros(2, 4, device=cuda),
+                    torch.zeros(1, 16, 2, 3, device=cuda))
+    with pytest.raises(NotImplementedError):
+        Cpab([2, 2], backend='numpy', device='cpu')
+    assert N.device_status() == 0
+
+
+def test_identity_and_zero_velocity(cuda):
+    """theta = 0 is the identity map; points stay where they are."""
+    from libcpab_gb300 import Cpab
+    for nc in ([5], [3, 3], [2, 2, 2]):
+        T = Cpab(nc, backend='pytorch', device='gpu')
+        grid = T.uniform_meshgrid([7] * len(nc))
+        out = T.transform_grid(grid, T.identity(3))
+        assert torch.equal(out, grid.expand(3, *grid.shape))
