@@ -47,7 +47,12 @@ def parse():
     ap.add_argument('--warmup', type=int, default=5)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
     ap.add_argument('--cpu-sample-images', type=int, default=1)
-    return ap.parse_args()
+    ap.add_argument('--batch', type=int, default=BATCH,
+                    help='images per step (the headline workload uses 64; smaller values '
+                         'are for profiling runs only)')
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    args = ap.parse_args()
+    return args
 
 
 def dist_env():
@@ -57,8 +62,9 @@ def dist_env():
     return rank, world, local
 
 
-def make_inputs(T, device, seed_offset=0):
+def make_inputs(T, device, seed_offset=0, batch=BATCH):
     d = T.get_theta_dim()
+    BATCH = batch
     g0 = torch.Generator().manual_seed(0 + seed_offset)
     g1 = torch.Generator().manual_seed(1 + seed_offset)
     g2 = torch.Generator().manual_seed(2 + seed_offset)
@@ -163,7 +169,7 @@ def run_gb300(args):
     device = torch.device('cuda', local)
     torch.cuda.set_device(device)
     T = Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True)
-    theta_h, data_h, target_h = make_inputs(T, device, seed_offset=10 * rank)
+    theta_h, data_h, target_h = make_inputs(T, device, seed_offset=10 * rank, batch=args.batch)
     theta_h, data_h, target_h = theta_h.pin_memory(), data_h.pin_memory(), target_h.pin_memory()
     theta = theta_h.to(device)
     data = data_h.to(device)
@@ -223,7 +229,7 @@ def run_gb300(args):
     out, grid = N.transform_data(NC, NSTEPS, lin, [SIZE, SIZE], E, data, save_grid=True)
     gout = (2.0 / out.numel()) * (out - target)
     ws_need = N.load().cpab_transform_data_backward_workspace(2, N._ints(NC), NSTEPS, 0,
-                                                               N._ints([SIZE, SIZE]), BATCH)
+                                                               N._ints([SIZE, SIZE]), args.batch)
     ws = torch.empty(ws_need, dtype=torch.uint8, device=device)
     t_fwd = time_events(lambda: N.transform_data(NC, NSTEPS, lin, [SIZE, SIZE], E, data,
                                                  save_grid=True), args.steps, flush)
@@ -234,7 +240,7 @@ def run_gb300(args):
     status = N.device_status()
 
     ms_max, ms_e2e_max = reduce_max([ms_step, ms_e2e], device)
-    pts = BATCH * SIZE * SIZE
+    pts = args.batch * SIZE * SIZE
     value = world * pts / (ms_max / 1e3)
     e2e_value = world * pts / (ms_e2e_max / 1e3)
 
@@ -255,7 +261,7 @@ def run_gb300(args):
             'config': {'workload': 'transform_data 2D tess [3,3] zero_boundary, 64 theta ~ '
                                    'N(0,0.25I), data [64,3,224,224] box-filtered U[0,1], '
                                    'MSE vs second warp, fwd + dtheta/d(data) bwd',
-                       'tess_size': NC, 'batch': BATCH, 'outsize': [SIZE, SIZE],
+                       'tess_size': NC, 'batch': args.batch, 'outsize': [SIZE, SIZE],
                        'nstepsolver': NSTEPS, 'gradient': params.gradient,
                        'l2': 'flushed before every timed iteration (%d MB write)'
                              % (2 * L2_BYTES // 2 ** 20),
@@ -366,7 +372,7 @@ def main():
         return
     res = run_gb300(args)
     if rank == 0 and res is not None:
-        if world == 1:
+        if world == 1 and not args.no_cpu_baseline:
             v, cores, sample = run_cpu_baseline(1, args.cpu_sample_images)
             res['cpu_baseline'] = {'value': v, 'unit': 'points/s', 'cores': cores,
                                    'kind': 'port', 'sample': sample}

@@ -94,6 +94,15 @@ CPAB_API int cpab_integrate(int ndim, const int *nc, int nsteps, const float *po
                    unsigned long long *ties, void *stream);
 
 /*
+ * cpab_integrate that also records the cell used at every step,
+ * cells [n_theta, nP, nsteps] int32 (diagnostics: boundary-tie analysis).
+ * No counterpart in the reference.
+ */
+CPAB_API int cpab_integrate_trace(int ndim, const int *nc, int nsteps, const float *points,
+                                  int broadcast, long long nP, const float *E, int n_theta,
+                                  float *out, int *cells, void *stream);
+
+/*
  * Workspace bytes needed by cpab_backward for this problem on the current
  * device (0 on invalid arguments; see cpab_last_error).
  */

@@ -31,6 +31,7 @@ _SIGS = {
     'cpab_cell_tables': ([_i, _c_int_p, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp], _i),
     'cpab_forward': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _vp], _i),
     'cpab_integrate': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _vp, _vp], _i),
+    'cpab_integrate_trace': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _vp, _vp], _i),
     'cpab_backward_workspace': ([_i, _c_int_p, _i, _ll, _i], _sz),
     'cpab_backward': ([_i, _c_int_p, _i, _i, _vp, _i, _ll, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp,
                        _vp, _sz, _vp, _vp], _i),
@@ -158,6 +159,22 @@ def integrate(nc, nsteps, points, E, ties=None):
     _check(load().cpab_integrate(ndim, _ints(nc), int(nsteps), _ptr(points), broadcast, nP,
                                  _ptr(E), n_theta, _ptr(out), _ptr(ties), _stream(points.device)))
     return out
+
+
+def integrate_trace(nc, nsteps, points, E):
+    """integrate() plus the cell of every step, [n_theta, nP, nsteps] int32."""
+    _require(points, 'points')
+    _require(E, 'E')
+    ndim = len(nc)
+    n_theta = E.shape[0]
+    broadcast = int(points.dim() == 3 and points.shape[0] == n_theta)
+    nP = points.shape[-1]
+    out = torch.empty((n_theta, ndim, nP), device=points.device, dtype=torch.float32)
+    cells = torch.empty((n_theta, nP, int(nsteps)), device=points.device, dtype=torch.int32)
+    _check(load().cpab_integrate_trace(ndim, _ints(nc), int(nsteps), _ptr(points), broadcast, nP,
+                                       _ptr(E), n_theta, _ptr(out), _ptr(cells),
+                                       _stream(points.device)))
+    return out, cells
 
 
 def backward(nc, nsteps, mode, points, A, E, basis, grad_out, want_dpoints=False, ties=None,

@@ -45,38 +45,19 @@ unsigned *device_error_word() {
     return g_err_ptr[dev];
 }
 
-// Tessellation constants, computed the way the reference computes them
-// (libcpab/core/cpab_ops.cpp:40-45, 108-110, 139-141).
+// Validate a tessellation and fill its constants (tess_init).
 int make_tess(int ndim, const int *nc, Tess *t) {
     if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3 (got %d)", ndim);
     if (!nc) return fail(CPAB_ERR_ARGUMENT, "nc is NULL");
     long long ncells = 1;
-    int ncmax = 1;
     for (int j = 0; j < ndim; ++j) {
         if (nc[j] < 1 || nc[j] > 4096)
             return fail(CPAB_ERR_ARGUMENT, "nc[%d] = %d out of range [1, 4096]", j, nc[j]);
         ncells *= nc[j];
-        ncmax = nc[j] > ncmax ? nc[j] : ncmax;
     }
     ncells *= (ndim == 1 ? 1 : ndim == 2 ? 4 : 5);
     if (ncells > 65535) return fail(CPAB_ERR_UNSUPPORTED, "too many cells (%lld > 65535)", ncells);
-    memset(t, 0, sizeof(*t));
-    t->ndim = ndim;
-    for (int j = 0; j < 3; ++j) {
-        const int n = j < ndim ? nc[j] : 1;
-        t->nc[j] = n;
-        t->inc[j] = (float)(1.0 / n);
-        t->rinc[j] = (float)(1.0 / (double)t->inc[j]);
-        t->wlim[j] = (float)n * t->inc[j];
-    }
-    t->nC = (int)ncells;
-    if (ndim == 3) {
-        t->clamp3[0] = (float)((double)((float)nc[0] * t->inc[0]) - 1e-8);
-        t->clamp3[1] = (float)((double)((float)nc[1] * t->inc[1]) - 1e-8);
-        t->clamp3[2] = (float)((double)((float)nc[2] * t->inc[0]) - 1e-8);  // inc_x, as the reference
-        for (int j = 0; j < 3; ++j) t->lim3[j] = t->clamp3[j] < 1.0f ? t->clamp3[j] : 1.0f;
-    }
-    t->eps = (float)((8.0 * ncmax + 16.0) * ldexp(1.0, -23));
+    tess_init(ndim, nc, t);
     return CPAB_OK;
 }
 
@@ -125,7 +106,8 @@ int cpab_cell_tables(int ndim, const int *nc, int nsteps, const float *theta, in
 
 static int integrate_common(int ndim, const int *nc, int nsteps, const float *points,
                             int broadcast, long long nP, const float *table, bool comp,
-                            int n_theta, float *out, unsigned long long *ties, void *stream) {
+                            int n_theta, float *out, int *trace, unsigned long long *ties,
+                            void *stream) {
     g_err[0] = 0;
     Tess t;
     int rc = make_tess(ndim, nc, &t);
@@ -136,21 +118,29 @@ static int integrate_common(int ndim, const int *nc, int nsteps, const float *po
     if (!points || !table || !out) return fail(CPAB_ERR_ARGUMENT, "points, table or out is NULL");
     unsigned *err = device_error_word();
     cudaError_t e = launch_integrate(t, nsteps, points, broadcast ? 1 : 0, nP, table, comp, n_theta,
-                                     out, ties, err, as_stream(stream));
+                                     out, trace, ties, err, as_stream(stream));
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "integrate launch");
 }
 
 int cpab_forward(int ndim, const int *nc, int nsteps, const float *points, int broadcast,
                  long long nP, const float *trels, int n_theta, float *out, void *stream) {
     return integrate_common(ndim, nc, nsteps, points, broadcast, nP, trels, false, n_theta, out,
-                            nullptr, stream);
+                            nullptr, nullptr, stream);
 }
 
 int cpab_integrate(int ndim, const int *nc, int nsteps, const float *points, int broadcast,
                    long long nP, const float *E, int n_theta, float *out,
                    unsigned long long *ties, void *stream) {
-    return integrate_common(ndim, nc, nsteps, points, broadcast, nP, E, true, n_theta, out, ties,
-                            stream);
+    return integrate_common(ndim, nc, nsteps, points, broadcast, nP, E, true, n_theta, out,
+                            nullptr, ties, stream);
+}
+
+int cpab_integrate_trace(int ndim, const int *nc, int nsteps, const float *points, int broadcast,
+                         long long nP, const float *E, int n_theta, float *out, int *cells,
+                         void *stream) {
+    if (!cells) return fail(CPAB_ERR_ARGUMENT, "cells is NULL");
+    return integrate_common(ndim, nc, nsteps, points, broadcast, nP, E, true, n_theta, out, cells,
+                            nullptr, stream);
 }
 
 size_t cpab_backward_workspace(int ndim, const int *nc, int nsteps, long long nP, int n_theta) {

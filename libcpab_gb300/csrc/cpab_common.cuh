@@ -4,17 +4,17 @@
 // -----------
 // The reference decides the cell of a point in double precision
 // (libcpab/core/cpab_ops.cu:21-227 for CUDA, libcpab/core/cpab_ops.cpp:26-184
-// for the CPU).  GB300 has a low FP64 rate, so lookups here run in FP32 and
-// are *certified*: the FP32 quantities (cell coordinate q = p/inc, its
-// fractional parts, and the sub-cell plane tests) carry a proven error bound
-// (|error| <= nc * 2^-23 for q in [0,nc]).  When every quantity that decides
-// the cell is farther than eps = 8*nc*2^-23 from its threshold, the FP32
-// decision equals the reference's double decision.  Otherwise (and for every
-// point outside the unit box, where the reference's out-of-domain rules
-// apply) the lookup is redone with an FP64 replica of the reference's
-// arithmetic.  The result is bit-identical to the reference lookup for every
-// float input; the FP64 branch is taken for a fraction ~1e-5 of in-domain
-// lookups and is counted when a counter is supplied.
+// for the CPU).  GB300 has a low FP64 rate, so lookups here run in FP32:
+//   * the cell index along each axis (floor(p/inc)) and the remainder
+//     p - i*inc are computed exactly with two FMAs (split_cell);
+//   * the sub-cell tests (triangle diagonals, tetrahedron planes) and the
+//     out-of-domain diagonal rules use FP32 values with a proven error bound;
+//     when a test lands within its margin of zero, the lookup is redone with
+//     an FP64 replica of the reference's arithmetic.
+// The result is bit-identical to the reference lookup for every float input.
+// The FP64 branch is taken only for genuine near-ties (a point within ~2e-6 of
+// a diagonal or plane, or non-finite input, or 3D points outside the box) and
+// is counted when a counter is supplied.
 //
 // Tables
 // ------
@@ -51,17 +51,53 @@ struct Tess {
     float rinc[3];    // (float)(1.0 / inc)  (approximate reciprocal, fast path only)
     float wlim[3];    // (float)nc * inc     (float product)
     float clamp3[3];  // 3D clamp limits (float)(nc*inc - 1e-8), z uses inc_x
-    float lim3[3];    // min(clamp3, 1.0f): fast-path upper bound in 3D
-    float eps;        // certified margin of the FP32 fast path
 };
 
-__device__ __forceinline__ int mymin_ref(int a, double b) { return !(b < a) ? a : (int)round(b); }
+// The lookup functions are host+device so that a host harness can check the
+// FP32 path against the FP64 replica on adversarial inputs.  Single IEEE
+// operations that must not be contracted into an FMA use these wrappers.
+#define CPAB_HD __host__ __device__
+#if defined(__CUDA_ARCH__)
+#define CPAB_MUL_RN(a, b) __fmul_rn((a), (b))
+#define CPAB_ADD_RN(a, b) __fadd_rn((a), (b))
+#define CPAB_SUB_RN(a, b) __fsub_rn((a), (b))
+#else
+#define CPAB_MUL_RN(a, b) ((a) * (b))
+#define CPAB_ADD_RN(a, b) ((a) + (b))
+#define CPAB_SUB_RN(a, b) ((a) - (b))
+#endif
+
+// Fill the tessellation constants exactly as the reference computes them
+// (libcpab/core/cpab_ops.cpp:40-45, 108-110, 139-141).  nc must hold ndim
+// positive counts; returns the number of cells.
+inline int tess_init(int ndim, const int *nc, Tess *t) {
+    *t = Tess();
+    t->ndim = ndim;
+    long long cells = 1;
+    for (int j = 0; j < 3; ++j) {
+        const int n = j < ndim ? nc[j] : 1;
+        t->nc[j] = n;
+        t->inc[j] = (float)(1.0 / n);
+        t->rinc[j] = (float)(1.0 / (double)t->inc[j]);
+        t->wlim[j] = (float)n * t->inc[j];
+        cells *= n;
+    }
+    t->nC = (int)(cells * (ndim == 1 ? 1 : ndim == 2 ? 4 : 5));
+    if (ndim == 3) {
+        t->clamp3[0] = (float)((double)((float)nc[0] * t->inc[0]) - 1e-8);
+        t->clamp3[1] = (float)((double)((float)nc[1] * t->inc[1]) - 1e-8);
+        t->clamp3[2] = (float)((double)((float)nc[2] * t->inc[0]) - 1e-8);  // inc_x, as the reference
+    }
+    return t->nC;
+}
+
+CPAB_HD inline int mymin_ref(int a, double b) { return !(b < a) ? a : (int)round(b); }
 
 // ------------------------------- 1D ---------------------------------------
 // Exact in FP32: floor(p * nc) with the float product, clamped
 // (cpab_ops.cu:14-19).
-__device__ __forceinline__ int cell_1d(float p, const Tess &t) {
-    float q = floorf(__fmul_rn(p, (float)t.nc[0]));
+CPAB_HD inline int cell_1d(float p, const Tess &t) {
+    float q = floorf(CPAB_MUL_RN(p, (float)t.nc[0]));
     int idx = (int)q;
     idx = max(0, min(idx, t.nc[0] - 1));
     return idx;
@@ -69,7 +105,7 @@ __device__ __forceinline__ int cell_1d(float p, const Tess &t) {
 
 // ------------------------------- 2D ---------------------------------------
 // FP64 replica of the reference's 2D lookup (cpab_ops.cpp:33-104).
-static __device__ __noinline__ int cell_2d_exact(float fpx, float fpy, const Tess &t) {
+static CPAB_HD __noinline__ int cell_2d_exact(float fpx, float fpy, const Tess &t) {
     const int nx = t.nc[0], ny = t.nc[1];
     const double px = fpx, py = fpy;
     const double ix = t.inc[0], iy = t.inc[1];
@@ -98,22 +134,80 @@ static __device__ __noinline__ int cell_2d_exact(float fpx, float fpy, const Tes
     return (1 - fx < fy) ? c + 1 : c;
 }
 
-// Certified FP32 lookup; falls back to the replica when not certain.
+// Exact floor(p / inc) and remainder p - i*inc for a float p >= 0, in FP32.
+// k = rint(p * rinc) is within 1/2 of the true quotient; the sign of
+// fma(-k, inc, p) (a single rounding of the exact p - k*inc, which keeps its
+// sign) decides between k and k-1; the remainder p - i*inc is representable
+// in FP32 (it is below inc and on inc's ulp grid), so the second fma returns
+// it exactly.  These are the reference's fmod/divide results
+// (cpab_ops.cpp:47-54), obtained without FP64.
+CPAB_HD inline void split_cell(float p, float inc, float rinc, int n, int &i, float &rem) {
+    const float k = rintf(p * rinc);
+    const float fi = (fmaf(-k, inc, p) >= 0.f) ? k : k - 1.f;
+    rem = fmaf(-fi, inc, p);
+    i = min((int)fi, n - 1);   // mymin: the index is capped, the remainder is not
+}
+
+// Margin of the FP32 sub-cell tests.  x = rem * rinc differs from the
+// reference's double x = rem / inc by at most 2^-22 (two roundings), so a
+// two-term test carries an error below 2^-20 and a three-term test below
+// 2^-19; decisions closer than these margins go to the FP64 replica.
+constexpr float kMargin2 = 1.9073486328125e-06f;   // 2^-19
+constexpr float kMargin3 = 3.814697265625e-06f;    // 2^-18
+
+// FP32 lookup with the reference's semantics; returns -1 when a decision is
+// within its error margin (the caller then uses the FP64 replica).
+CPAB_HD inline int cell_2d_fast(float px, float py, const Tess &t) {
+    if (!(fabsf(px) <= 1e30f) || !(fabsf(py) <= 1e30f)) return -1;   // NaN / Inf / huge
+    const int nx = t.nc[0], ny = t.nc[1];
+    const float wx = t.wlim[0], wy = t.wlim[1];
+    int i, j;
+    float xm = 0.f, ym = 0.f;
+    if (px > 0.f && px < wx) split_cell(px, t.inc[0], t.rinc[0], nx, i, xm);
+    else i = (px <= 0.f) ? 0 : nx - 1;
+    if (py > 0.f && py < wy) split_cell(py, t.inc[1], t.rinc[1], ny, j, ym);
+    else j = (py <= 0.f) ? 0 : ny - 1;
+    const int c = 4 * (i + j * nx);
+    const float ax = px * t.rinc[0], ay = py * t.rinc[1];   // px/inc_x, py/inc_y (rel. err 2^-23)
+    const float tol = (fabsf(ax) + fabsf(ay) + (float)(nx + ny)) * 9.5367431640625e-07f + kMargin2;
+    if (px <= 0.f) {                       // left of the domain (cpab_ops.cpp:58-67)
+        if (py <= 0.f) {
+            const float d = ay - ax;
+            if (fabsf(d) <= tol) return -1;
+            return d < 0.f ? c : c + 3;
+        }
+        if (py >= wy) {
+            const float d = (ay - (float)ny) + ax;
+            if (fabsf(d) <= tol) return -1;
+            return d > 0.f ? c + 2 : c + 3;
+        }
+        return c + 3;
+    }
+    if (px >= wx) {                        // right of the domain (cpab_ops.cpp:70-79)
+        if (py <= 0.f) {
+            const float d = -ay - (ax - (float)nx);
+            if (fabsf(d) <= tol) return -1;
+            return d > 0.f ? c : c + 1;
+        }
+        if (py >= wy) {
+            const float d = (ay - (float)ny) - (ax - (float)nx);
+            if (fabsf(d) <= tol) return -1;
+            return d > 0.f ? c + 2 : c + 1;
+        }
+        return c + 1;
+    }
+    if (py <= 0.f) return c;               // above
+    if (py >= wy) return c + 2;            // below
+    const float x = xm * t.rinc[0], y = ym * t.rinc[1];
+    const float dxy = x - y, sxy = (x + y) - 1.f;
+    if (fabsf(dxy) <= kMargin2 || fabsf(sxy) <= kMargin2) return -1;
+    return c + (dxy < 0.f ? (sxy > 0.f ? 2 : 3) : (sxy > 0.f ? 1 : 0));
+}
+
 __device__ __forceinline__ int cell_2d(float px, float py, const Tess &t,
                                        unsigned long long *ties) {
-    const float eps = t.eps;
-    if (px > 0.f && px < t.wlim[0] && py > 0.f && py < t.wlim[1]) {
-        const float qx = px * t.rinc[0], qy = py * t.rinc[1];
-        const float gx = floorf(qx), gy = floorf(qy);
-        const float fx = qx - gx, fy = qy - gy;
-        const float dxy = fx - fy, sxy = (fx + fy) - 1.f;
-        const bool ok = (fx > eps) & (fx < 1.f - eps) & (fy > eps) & (fy < 1.f - eps) &
-                        (fabsf(dxy) > eps) & (fabsf(sxy) > eps);
-        if (ok) {
-            const int c = 4 * ((int)gx + (int)gy * t.nc[0]);
-            return c + (dxy < 0.f ? (sxy > 0.f ? 2 : 3) : (sxy > 0.f ? 1 : 0));
-        }
-    }
+    const int c = cell_2d_fast(px, py, t);
+    if (c >= 0) return c;
     if (ties) atomicAdd(ties, 1ull);
     return cell_2d_exact(px, py, t);
 }
@@ -122,21 +216,21 @@ __device__ __forceinline__ int cell_2d(float px, float py, const Tess &t,
 // FP64 replica of the reference's 3D lookup (cpab_ops.cpp:106-184), including
 // the push-inside rule that tests only x and y, and the z clamp that uses
 // inc_x.
-static __device__ __noinline__ int cell_3d_exact(float p0, float p1, float p2, const Tess &t) {
+static CPAB_HD __noinline__ int cell_3d_exact(float p0, float p1, float p2, const Tess &t) {
     const int nx = t.nc[0], ny = t.nc[1], nz = t.nc[2];
     const float ix = t.inc[0], iy = t.inc[1], iz = t.inc[2];
     float q0 = p0, q1 = p1, q2 = p2;
     if (q0 < 0.0 || q0 > 1.0 || q1 < 0.0 || q1 > 1.0) {
         const float h = 0.5f;
-        q0 = __fsub_rn(q0, h); q1 = __fsub_rn(q1, h); q2 = __fsub_rn(q2, h);
+        q0 = CPAB_SUB_RN(q0, h); q1 = CPAB_SUB_RN(q1, h); q2 = CPAB_SUB_RN(q2, h);
         const float a0 = fabsf(q0), a1 = fabsf(q1), a2 = fabsf(q2);
-        const float s0 = (a0 < a1 && a0 < a2) ? __fmul_rn(h, ix) : 0.0f;
-        const float s1 = (a1 < a0 && a0 < a2) ? __fmul_rn(h, iy) : 0.0f;
-        const float s2 = (a2 < a0 && a0 < a1) ? __fmul_rn(h, iz) : 0.0f;
-        if (a0 > h) q0 = copysignf(__fsub_rn(h, s0), q0);
-        if (a1 > h) q1 = copysignf(__fsub_rn(h, s1), q1);
-        if (a2 > h) q2 = copysignf(__fsub_rn(h, s2), q2);
-        q0 = __fadd_rn(q0, h); q1 = __fadd_rn(q1, h); q2 = __fadd_rn(q2, h);
+        const float s0 = (a0 < a1 && a0 < a2) ? CPAB_MUL_RN(h, ix) : 0.0f;
+        const float s1 = (a1 < a0 && a0 < a2) ? CPAB_MUL_RN(h, iy) : 0.0f;
+        const float s2 = (a2 < a0 && a0 < a1) ? CPAB_MUL_RN(h, iz) : 0.0f;
+        if (a0 > h) q0 = copysignf(CPAB_SUB_RN(h, s0), q0);
+        if (a1 > h) q1 = copysignf(CPAB_SUB_RN(h, s1), q1);
+        if (a2 > h) q2 = copysignf(CPAB_SUB_RN(h, s2), q2);
+        q0 = CPAB_ADD_RN(q0, h); q1 = CPAB_ADD_RN(q1, h); q2 = CPAB_ADD_RN(q2, h);
     }
     const float zero = 0.0f;
     float c0 = (zero < q0) ? q0 : zero; if (q0 != q0) c0 = zero;
@@ -164,38 +258,49 @@ static __device__ __noinline__ int cell_3d_exact(float p0, float p1, float p2, c
     return c;
 }
 
-__device__ __forceinline__ int cell_3d(float p0, float p1, float p2, const Tess &t,
-                                       unsigned long long *ties) {
-    const float eps = t.eps;
-    if (p0 > 0.f && p0 < t.lim3[0] && p1 > 0.f && p1 < t.lim3[1] && p2 > 0.f &&
-        p2 < t.lim3[2]) {
-        const float q0 = p0 * t.rinc[0], q1 = p1 * t.rinc[1], q2 = p2 * t.rinc[2];
-        const float g0 = floorf(q0), g1 = floorf(q1), g2 = floorf(q2);
-        float x = q0 - g0, y = q1 - g1;
-        const float z = q2 - g2;
-        bool ok = (x > eps) & (x < 1.f - eps) & (y > eps) & (y < 1.f - eps) & (z > eps) &
-                  (z < 1.f - eps);
-        if (ok) {
-            const int i = (int)g0, j = (int)g1, k = (int)g2;
-            const bool flip = ((i ^ j ^ k) & 1) != 0;   // same parity rule as the reference
-            if (flip) { const float tmp = x; x = y; y = 1.f - tmp; }
-            const int c = 5 * (i + j * t.nc[0] + k * t.nc[0] * t.nc[1]);
-            const float t1 = (z - x) - y;
-            if (fabsf(t1) > eps) {
-                if (t1 > 0.f) return c + 1;
-                const float t2 = ((x + y) + z) - 2.f;
-                if (fabsf(t2) > eps) {
-                    if (t2 > 0.f) return c + 2;
-                    const float t3 = (y - x) - z;
-                    if (fabsf(t3) > eps) {
-                        if (t3 > 0.f) return c + 3;
-                        const float t4 = (x - y) - z;
-                        if (fabsf(t4) > eps) return (t4 > 0.f) ? c + 4 : c;
-                    }
+CPAB_HD inline int cell_3d_fast(float p0, float p1, float p2, const Tess &t) {
+    // With x and y in [0,1] the push-inside rule does not apply; the
+    // reference then clamps each coordinate to [0, clamp3] (in float) and
+    // splits it, which split_cell does exactly.  Only the tetrahedron plane
+    // tests need a margin.
+    if (!(fabsf(p0) <= 1e30f) || !(fabsf(p1) <= 1e30f) || !(fabsf(p2) <= 1e30f)) return -1;
+    if (p0 >= 0.f && p0 <= 1.f && p1 >= 0.f && p1 <= 1.f) {
+        const float c0 = (p0 < t.clamp3[0]) ? p0 : t.clamp3[0];
+        const float c1 = (p1 < t.clamp3[1]) ? p1 : t.clamp3[1];
+        float c2 = (0.f < p2) ? p2 : 0.f;
+        c2 = (c2 < t.clamp3[2]) ? c2 : t.clamp3[2];
+        int i, j, k;
+        float r0, r1, r2;
+        split_cell(c0, t.inc[0], t.rinc[0], t.nc[0], i, r0);
+        split_cell(c1, t.inc[1], t.rinc[1], t.nc[1], j, r1);
+        split_cell(c2, t.inc[2], t.rinc[2], t.nc[2], k, r2);
+        float x = r0 * t.rinc[0], y = r1 * t.rinc[1];
+        const float z = r2 * t.rinc[2];
+        const bool flip = ((i ^ j ^ k) & 1) != 0;   // the reference's parity rule
+        if (flip) { const float tmp = x; x = y; y = 1.f - tmp; }
+        const int c = 5 * (i + j * t.nc[0] + k * t.nc[0] * t.nc[1]);
+        const float t1 = (z - x) - y;
+        if (fabsf(t1) > kMargin3) {
+            if (t1 > 0.f) return c + 1;
+            const float t2 = ((x + y) + z) - 2.f;
+            if (fabsf(t2) > kMargin3) {
+                if (t2 > 0.f) return c + 2;
+                const float t3 = (y - x) - z;
+                if (fabsf(t3) > kMargin3) {
+                    if (t3 > 0.f) return c + 3;
+                    const float t4 = (x - y) - z;
+                    if (fabsf(t4) > kMargin3) return (t4 > 0.f) ? c + 4 : c;
                 }
             }
         }
     }
+    return -1;
+}
+
+__device__ __forceinline__ int cell_3d(float p0, float p1, float p2, const Tess &t,
+                                       unsigned long long *ties) {
+    const int c = cell_3d_fast(p0, p1, p2, t);
+    if (c >= 0) return c;
     if (ties) atomicAdd(ties, 1ull);
     return cell_3d_exact(p0, p1, p2, t);
 }

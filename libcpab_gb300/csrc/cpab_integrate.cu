@@ -22,7 +22,7 @@ template <int N, bool COMP, int PPT>
 __global__ void __launch_bounds__(256)
     k_integrate(Tess t, int nsteps, const float *__restrict__ points, int broadcast, long long nP,
                 const float *__restrict__ table, int tiles, float *__restrict__ out,
-                unsigned long long *ties, unsigned *err) {
+                int *__restrict__ trace, unsigned long long *ties, unsigned *err) {
     constexpr int P = N * (N + 1);
     extern __shared__ float4 smem4[];
     __shared__ uint64_t bar;
@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(256)
                 raise_error(err, kErrBadCell);
                 c = 0;
             }
+            if (trace && idx[j] < nP) trace[((long long)th * nP + idx[j]) * nsteps + s] = c;
             float M[P], y[N];
             load_cell<N>(tab, c, M);
             affine_apply<N>(M, p[j], y);
@@ -69,8 +70,8 @@ __global__ void __launch_bounds__(256)
 template <int N, bool COMP, int PPT>
 static cudaError_t launch_integrate_t(const Tess &t, int nsteps, const float *points,
                                       int broadcast, long long nP, const float *table,
-                                      int n_theta, float *out, unsigned long long *ties,
-                                      unsigned *err, cudaStream_t s) {
+                                      int n_theta, float *out, int *trace,
+                                      unsigned long long *ties, unsigned *err, cudaStream_t s) {
     constexpr int block = 256;
     const long long per = (long long)block * PPT;
     const int tiles = (int)((nP + per - 1) / per);
@@ -85,26 +86,26 @@ static cudaError_t launch_integrate_t(const Tess &t, int nsteps, const float *po
         if (e != cudaSuccess) return e;
     }
     kern<<<(unsigned)grid, block, smem, s>>>(t, nsteps, points, broadcast, nP, table, tiles, out,
-                                             ties, err);
+                                             trace, ties, err);
     return cudaGetLastError();
 }
 
 cudaError_t launch_integrate(const Tess &t, int nsteps, const float *points, int broadcast,
                              long long nP, const float *table, bool compensated, int n_theta,
-                             float *out, unsigned long long *ties, unsigned *err,
+                             float *out, int *trace, unsigned long long *ties, unsigned *err,
                              cudaStream_t s) {
     // Two points per thread once there is enough work to fill the GPU twice.
     const bool two = (long long)n_theta * nP >= (long long)num_sms() * 2048 * 2;
 #define CPAB_INTEGRATE(N)                                                                        \
     if (compensated)                                                                             \
         return two ? launch_integrate_t<N, true, 2>(t, nsteps, points, broadcast, nP, table,    \
-                                                    n_theta, out, ties, err, s)                  \
+                                                    n_theta, out, trace, ties, err, s)                  \
                    : launch_integrate_t<N, true, 1>(t, nsteps, points, broadcast, nP, table,    \
-                                                    n_theta, out, ties, err, s);                 \
+                                                    n_theta, out, trace, ties, err, s);                 \
     return two ? launch_integrate_t<N, false, 2>(t, nsteps, points, broadcast, nP, table,       \
-                                                 n_theta, out, ties, err, s)                     \
+                                                 n_theta, out, trace, ties, err, s)                     \
                : launch_integrate_t<N, false, 1>(t, nsteps, points, broadcast, nP, table,       \
-                                                 n_theta, out, ties, err, s);
+                                                 n_theta, out, trace, ties, err, s);
     switch (t.ndim) {
         case 1: { CPAB_INTEGRATE(1) }
         case 2: { CPAB_INTEGRATE(2) }

@@ -16,10 +16,11 @@ cudaError_t launch_cell_tables(const Tess &t, int nsteps, const float *theta, in
                                cudaStream_t s);
 
 // Forward integration.  `table` holds T (compensated=false, p <- T p~) or
-// E (compensated=true, p <- p + E p~).
+// E (compensated=true, p <- p + E p~).  trace (nullable) receives the cell of
+// every step, [n_theta, nP, nsteps].
 cudaError_t launch_integrate(const Tess &t, int nsteps, const float *points, int broadcast,
                              long long nP, const float *table, bool compensated, int n_theta,
-                             float *out, unsigned long long *ties, unsigned *err,
+                             float *out, int *trace, unsigned long long *ties, unsigned *err,
                              cudaStream_t s);
 
 cudaError_t launch_findcellidx(const Tess &t, const float *points, long long nP, int *out,

@@ -340,20 +340,21 @@ def numpy_transform_grid(basis, theta, points, nc, nsteps=50, return_cells=False
     Ph = np.concatenate([P, np.ones((P.shape[0], 1))], axis=1)[:, :, None]
     Tf = T.reshape(n_theta * nC, ndim + 1, ndim + 1)
     base = np.repeat(np.arange(n_theta) * nC, nP)
-    cells = []
-    margin = np.full(n_theta * nP, np.inf)
+    cells, margins = [], []
     for _ in range(nsteps):
         c = numpy_findcellidx(ndim, Ph[:, :ndim, 0].T, nc)
         if return_margin:
-            margin = np.minimum(margin, decision_margin(ndim, Ph[:, :ndim, 0].T, nc))
+            margins.append(decision_margin(ndim, Ph[:, :ndim, 0].T, nc))
         cells.append(c)
         Ph = np.matmul(Tf[c + base], Ph)
     out = Ph[:, :ndim, 0].reshape(n_theta, nP, ndim).transpose(0, 2, 1)
     res = [out]
     if return_cells:
         res.append(np.stack(cells, axis=1).reshape(n_theta, nP, nsteps))
-    if return_margin:
-        res.append(margin.reshape(n_theta, nP))
+    if return_margin == 'steps':
+        res.append(np.stack(margins, axis=1).reshape(n_theta, nP, nsteps))
+    elif return_margin:
+        res.append(np.min(np.stack(margins, axis=1), axis=1).reshape(n_theta, nP))
     return res[0] if len(res) == 1 else tuple(res)
 
 

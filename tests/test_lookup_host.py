@@ -1,0 +1,95 @@
+"""The FP32 cell lookup of the kernels, compiled for the host and checked on
+adversarial points: wherever the FP32 path answers, it must equal the FP64
+replica, and the FP64 replica must equal the C oracle (itself bit-identical to
+the reference's cpab_ops.cpp, see test_cpu.py).  Runs on the CPU; needs nvcc.
+"""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+NVCC = shutil.which('nvcc') or '/usr/local/cuda/bin/nvcc'
+
+
+@pytest.fixture(scope='module')
+def harness(tmp_path_factory):
+    if not os.path.exists(NVCC):
+        pytest.skip('nvcc not available')
+    out = str(tmp_path_factory.mktemp('lookup') / 'lookup_check')
+    subprocess.check_call([NVCC, '-O2', '-std=c++17', '-o', out,
+                           os.path.join(REPO, 'tests', 'lookup_check.cu')])
+    return out
+
+
+def run(harness, tmp_path, nc, P):
+    P = np.ascontiguousarray(P, dtype=np.float32)
+    ndim, n = P.shape
+    hdr = np.array([ndim] + list(nc) + [1] * (3 - len(nc)), dtype=np.int32)
+    fin, fout = str(tmp_path / 'in.bin'), str(tmp_path / 'out.bin')
+    with open(fin, 'wb') as f:
+        f.write(hdr.tobytes())
+        f.write(np.int64(n).tobytes())
+        f.write(P.tobytes())
+    subprocess.check_call([harness, fin, fout])
+    r = np.fromfile(fout, dtype=np.int32)
+    return r[:n], r[n:]
+
+
+def adversarial(nc, rng, n=400000):
+    """Faces (exact float multiples of the reference's float inc and of k/nc,
+    +-1..3 ulp), sub-cell diagonals/planes, corners, and out-of-domain points."""
+    ndim = len(nc)
+    P = rng.uniform(-0.2, 1.2, (ndim, n)).astype(np.float32)
+    m = n // 6
+    for j in range(ndim):
+        inc32 = np.float32(1.0 / nc[j])
+        k = rng.integers(0, nc[j] + 1, m)
+        base = np.where(rng.random(m) < 0.5, (k * inc32).astype(np.float32),
+                        (k / nc[j]).astype(np.float32))
+        steps = rng.integers(-3, 4, m)
+        v = base.copy()
+        for s in range(1, 4):
+            v = np.where(steps >= s, np.nextafter(v, np.float32(3)), v)
+            v = np.where(steps <= -s, np.nextafter(v, np.float32(-3)), v)
+        P[j, j * m:(j + 1) * m] = v
+    # points on the square diagonals / tet planes: x-frac == y-frac, x+y == 1, ...
+    i0 = ndim * m
+    t = rng.random(m).astype(np.float64)
+    cx = rng.integers(0, nc[0], m)
+    cy = rng.integers(0, nc[1] if ndim > 1 else 1, m)
+    P[0, i0:i0 + m] = ((cx + t) / nc[0]).astype(np.float32)
+    if ndim > 1:
+        sel = rng.random(m) < 0.5
+        fy = np.where(sel, t, 1 - t)
+        P[1, i0:i0 + m] = ((cy + fy) / nc[1]).astype(np.float32)
+    if ndim > 2:
+        P[2, i0:i0 + m] = ((rng.integers(0, nc[2], m) + np.where(sel, t, 1 - t)) / nc[2]).astype(np.float32)
+    # zero-boundary style points hugging the domain faces
+    i1 = i0 + m
+    P[:, i1:i1 + m] = rng.random((ndim, m)).astype(np.float32)
+    face = rng.integers(0, ndim, m)
+    val = rng.choice(np.array([0.0, -0.0, 1e-30, 1e-12, -1e-12, 1.0, np.nextafter(np.float32(1), np.float32(0))],
+                              dtype=np.float32), m)
+    P[face, i1 + np.arange(m)] = val
+    return P
+
+
+@pytest.mark.parametrize('nc', [[50], [100], [3, 3], [8, 8], [4, 4], [7, 5], [2, 3],
+                                [2, 2, 2], [4, 4, 4], [3, 5, 2]])
+def test_fp32_lookup_agrees_with_fp64_replica_and_oracle(nc, harness, tmp_path, oracle):
+    rng = np.random.default_rng(sum(nc) * 7919 + len(nc))
+    P = adversarial(nc, rng)
+    fast, exact = run(harness, tmp_path, nc, P)
+    ref = oracle.findcellidx(nc, P)
+    assert np.array_equal(exact, ref), 'FP64 replica differs from the oracle'
+    answered = fast >= 0
+    bad = np.nonzero(answered & (fast != exact))[0]
+    assert bad.size == 0, 'FP32 lookup wrong at %s' % P[:, bad[:5]].T
+    # on random in-domain points the FP64 path is (almost) never needed
+    U = rng.random((len(nc), 200000)).astype(np.float32)
+    f2, _ = run(harness, tmp_path, nc, U)
+    assert (f2 < 0).mean() < 1e-4
