@@ -205,10 +205,14 @@ def _np_round_min(a, b):
     return np.where(a < b, a, np.round(b))
 
 
-def numpy_findcellidx(ndim, p, nc):
-    """Vectorised cell lookup with the numpy backend's semantics
-    (libcpab/numpy/findcellidx.py:22-150; in 3D it also tests z when deciding
-    whether a point is outside, unlike the C++/CUDA lookup)."""
+def numpy_findcellidx(ndim, p, nc, semantics='numpy'):
+    """Vectorised FP64 cell lookup.
+
+    semantics='numpy': the reference's numpy backend
+    (libcpab/numpy/findcellidx.py:22-150); in 3D it tests z when deciding
+    whether a point is outside.  semantics='cpp': the reference's C++/CUDA
+    rules in 3D (libcpab/core/cpab_ops.cpp:118-141): z is not part of the
+    outside test and z is clamped with nz*inc_x."""
     p = np.array(p, dtype=np.float64, copy=True)
     if ndim == 1:
         nx = nc[0]
@@ -241,7 +245,9 @@ def numpy_findcellidx(ndim, p, nc):
         idx = idx + 2 * (c2 | c5 | c7 | c8) + 3 * (c3 | c9) + 1 * (c6 | c10)
         return idx.astype(np.int64)
     nx, ny, nz = nc
-    outside = ((p[0] < 0) | (p[0] > 1) | (p[1] < 0) | (p[1] > 1) | (p[2] < 0) | (p[2] > 1))
+    outside = (p[0] < 0) | (p[0] > 1) | (p[1] < 0) | (p[1] > 1)
+    if semantics == 'numpy':
+        outside = outside | (p[2] < 0) | (p[2] > 1)
     ix, iy, iz = 1.0 / nx, 1.0 / ny, 1.0 / nz
     h = 0.5
     q = p[:, outside] - h
@@ -255,7 +261,7 @@ def numpy_findcellidx(ndim, p, nc):
     p[:, outside] = q + h
     p0 = np.minimum(nx * ix - 1e-8, np.maximum(0.0, p[0]))
     p1 = np.minimum(ny * iy - 1e-8, np.maximum(0.0, p[1]))
-    p2 = np.minimum(nz * iz - 1e-8, np.maximum(0.0, p[2]))
+    p2 = np.minimum(nz * (iz if semantics == 'numpy' else ix) - 1e-8, np.maximum(0.0, p[2]))
     xm, ym, zm = np.mod(p0, ix), np.mod(p1, iy), np.mod(p2, iz)
     i = _np_round_min(nx - 1, (p0 - xm) / ix)
     j = _np_round_min(ny - 1, (p1 - ym) / iy)
@@ -322,8 +328,9 @@ def decision_margin(ndim, p, nc):
 
 
 def numpy_transform_grid(basis, theta, points, nc, nsteps=50, return_cells=False,
-                         return_margin=False):
-    """FP64 fixed-step integration with the numpy backend's semantics.
+                         return_margin=False, semantics='numpy'):
+    """FP64 fixed-step integration with the numpy backend's semantics
+    (semantics='cpp' uses the C++/CUDA cell rules, see numpy_findcellidx).
 
     return_margin adds, per point, the smallest decision_margin met along the
     trajectory ([n_theta, nP])."""
@@ -342,7 +349,7 @@ def numpy_transform_grid(basis, theta, points, nc, nsteps=50, return_cells=False
     base = np.repeat(np.arange(n_theta) * nC, nP)
     cells, margins = [], []
     for _ in range(nsteps):
-        c = numpy_findcellidx(ndim, Ph[:, :ndim, 0].T, nc)
+        c = numpy_findcellidx(ndim, Ph[:, :ndim, 0].T, nc, semantics)
         if return_margin:
             margins.append(decision_margin(ndim, Ph[:, :ndim, 0].T, nc))
         cells.append(c)
