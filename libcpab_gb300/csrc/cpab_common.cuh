@@ -6,15 +6,16 @@
 // (libcpab/core/cpab_ops.cu:21-227 for CUDA, libcpab/core/cpab_ops.cpp:26-184
 // for the CPU).  GB300 has a low FP64 rate, so lookups here run in FP32:
 //   * the cell index along each axis (floor(p/inc)) and the remainder
-//     p - i*inc are computed exactly with two FMAs (split_cell);
-//   * the sub-cell tests (triangle diagonals, tetrahedron planes) and the
-//     out-of-domain diagonal rules use FP32 values with a proven error bound;
-//     when a test lands within its margin of zero, the lookup is redone with
-//     an FP64 replica of the reference's arithmetic.
+//     p - i*inc are computed exactly with two FMAs (split_exact);
+//   * the sub-cell tests (triangle diagonals, tetrahedron planes; in 2D also
+//     the out-of-domain rules, which are the same tests on the edge square)
+//     use FP32 values with a proven error bound; when a test lands within its
+//     margin of zero, the lookup is redone with an FP64 replica of the
+//     reference's arithmetic.
 // The result is bit-identical to the reference lookup for every float input.
 // The FP64 branch is taken only for genuine near-ties (a point within ~2e-6 of
-// a diagonal or plane, or non-finite input, or 3D points outside the box) and
-// is counted when a counter is supplied.
+// a diagonal or plane), non-finite input, and 3D points outside the unit box
+// in x or y; it is counted when a counter is supplied.
 //
 // Tables
 // ------
@@ -51,6 +52,7 @@ struct Tess {
     float rinc[3];    // (float)(1.0 / inc)  (approximate reciprocal, fast path only)
     float wlim[3];    // (float)nc * inc     (float product)
     float clamp3[3];  // 3D clamp limits (float)(nc*inc - 1e-8), z uses inc_x
+    int band[3];      // 1 if (float)(nc*inc) > nc*inc: floats in [nc*inc, wlim) exist
 };
 
 // The lookup functions are host+device so that a host harness can check the
@@ -80,6 +82,7 @@ inline int tess_init(int ndim, const int *nc, Tess *t) {
         t->inc[j] = (float)(1.0 / n);
         t->rinc[j] = (float)(1.0 / (double)t->inc[j]);
         t->wlim[j] = (float)n * t->inc[j];
+        t->band[j] = (double)t->wlim[j] > (double)n * (double)t->inc[j];
         cells *= n;
     }
     t->nC = (int)(cells * (ndim == 1 ? 1 : ndim == 2 ? 4 : 5));
@@ -134,73 +137,51 @@ static CPAB_HD __noinline__ int cell_2d_exact(float fpx, float fpy, const Tess &
     return (1 - fx < fy) ? c + 1 : c;
 }
 
-// Exact floor(p / inc) and remainder p - i*inc for a float p >= 0, in FP32.
+// Exact floor(p / inc), as a float, and the remainder p - fi*inc, in FP32.
 // k = rint(p * rinc) is within 1/2 of the true quotient; the sign of
-// fma(-k, inc, p) (a single rounding of the exact p - k*inc, which keeps its
-// sign) decides between k and k-1; the remainder p - i*inc is representable
-// in FP32 (it is below inc and on inc's ulp grid), so the second fma returns
-// it exactly.  These are the reference's fmod/divide results
-// (cpab_ops.cpp:47-54), obtained without FP64.
-CPAB_HD inline void split_cell(float p, float inc, float rinc, int n, int &i, float &rem) {
+// fma(-k, inc, p) (one rounding of the exact p - k*inc, which keeps its sign)
+// decides between k and k-1.  For p >= 0 the remainder lies in [0, inc) on
+// inc's ulp grid, so the second fma returns it exactly: these are the
+// reference's fmod/divide results (cpab_ops.cpp:47-54) without FP64.
+CPAB_HD inline void split_exact(float p, float inc, float rinc, float &fi, float &rem) {
     const float k = rintf(p * rinc);
-    const float fi = (fmaf(-k, inc, p) >= 0.f) ? k : k - 1.f;
+    fi = (fmaf(-k, inc, p) >= 0.f) ? k : k - 1.f;
     rem = fmaf(-fi, inc, p);
-    i = min((int)fi, n - 1);   // mymin: the index is capped, the remainder is not
 }
 
-// Margin of the FP32 sub-cell tests.  x = rem * rinc differs from the
-// reference's double x = rem / inc by at most 2^-22 (two roundings), so a
-// two-term test carries an error below 2^-20 and a three-term test below
-// 2^-19; decisions closer than these margins go to the FP64 replica.
+// Margin of the FP32 sub-cell tests.  A sub-cell coordinate rem*rinc differs
+// from the reference's double rem/inc by at most 2^-22; a two-term test then
+// carries an error below (1+|x|+|y|) 2^-21 and a three-term test below
+// 2^-20.  Decisions closer than these margins go to the FP64 replica.
 constexpr float kMargin2 = 1.9073486328125e-06f;   // 2^-19
 constexpr float kMargin3 = 3.814697265625e-06f;    // 2^-18
 
-// FP32 lookup with the reference's semantics; returns -1 when a decision is
-// within its error margin (the caller then uses the FP64 replica).
+// FP32 2D lookup with the reference's semantics for every finite point;
+// returns -1 when a decision is within its error margin.
+//
+// Outside the domain the reference applies its left/right/above/below rules
+// (cpab_ops.cpp:57-90).  Each of them is the in-square triangle test applied
+// to the edge square with unclamped sub-cell coordinates, e.g. left of and
+// above the domain it takes triangle 0 iff py/iy < px/ix, i.e. y < x, which
+// is what the test below gives there.  So one formula serves all points: the
+// square is the clamped exact split, the coordinates are measured from it,
+// and only exact ties (margin) differ.  NaN/Inf fail the margin test.
 CPAB_HD inline int cell_2d_fast(float px, float py, const Tess &t) {
-    if (!(fabsf(px) <= 1e30f) || !(fabsf(py) <= 1e30f)) return -1;   // NaN / Inf / huge
-    const int nx = t.nc[0], ny = t.nc[1];
-    const float wx = t.wlim[0], wy = t.wlim[1];
-    int i, j;
-    float xm = 0.f, ym = 0.f;
-    if (px > 0.f && px < wx) split_cell(px, t.inc[0], t.rinc[0], nx, i, xm);
-    else i = (px <= 0.f) ? 0 : nx - 1;
-    if (py > 0.f && py < wy) split_cell(py, t.inc[1], t.rinc[1], ny, j, ym);
-    else j = (py <= 0.f) ? 0 : ny - 1;
-    const int c = 4 * (i + j * nx);
-    const float ax = px * t.rinc[0], ay = py * t.rinc[1];   // px/inc_x, py/inc_y (rel. err 2^-23)
-    const float tol = (fabsf(ax) + fabsf(ay) + (float)(nx + ny)) * 9.5367431640625e-07f + kMargin2;
-    if (px <= 0.f) {                       // left of the domain (cpab_ops.cpp:58-67)
-        if (py <= 0.f) {
-            const float d = ay - ax;
-            if (fabsf(d) <= tol) return -1;
-            return d < 0.f ? c : c + 3;
-        }
-        if (py >= wy) {
-            const float d = (ay - (float)ny) + ax;
-            if (fabsf(d) <= tol) return -1;
-            return d > 0.f ? c + 2 : c + 3;
-        }
-        return c + 3;
-    }
-    if (px >= wx) {                        // right of the domain (cpab_ops.cpp:70-79)
-        if (py <= 0.f) {
-            const float d = -ay - (ax - (float)nx);
-            if (fabsf(d) <= tol) return -1;
-            return d > 0.f ? c : c + 1;
-        }
-        if (py >= wy) {
-            const float d = (ay - (float)ny) - (ax - (float)nx);
-            if (fabsf(d) <= tol) return -1;
-            return d > 0.f ? c + 2 : c + 1;
-        }
-        return c + 1;
-    }
-    if (py <= 0.f) return c;               // above
-    if (py >= wy) return c + 2;            // below
-    const float x = xm * t.rinc[0], y = ym * t.rinc[1];
+    float fi, ri, fj, rj;
+    split_exact(px, t.inc[0], t.rinc[0], fi, ri);
+    split_exact(py, t.inc[1], t.rinc[1], fj, rj);
+    const float ci = fminf(fmaxf(fi, 0.f), (float)(t.nc[0] - 1));
+    const float cj = fminf(fmaxf(fj, 0.f), (float)(t.nc[1] - 1));
+    // In-domain points past nc*inc (possible only when the float product
+    // nc*inc rounds above it) get the fmod remainder, not the continuous one.
+    if ((t.band[0] && fi > ci && px < t.wlim[0]) || (t.band[1] && fj > cj && py < t.wlim[1]))
+        return -1;
+    const float x = fmaf(ri, t.rinc[0], fi - ci);
+    const float y = fmaf(rj, t.rinc[1], fj - cj);
     const float dxy = x - y, sxy = (x + y) - 1.f;
-    if (fabsf(dxy) <= kMargin2 || fabsf(sxy) <= kMargin2) return -1;
+    const float m = kMargin2 * ((1.f + fabsf(x)) + fabsf(y));
+    if (!(fabsf(dxy) > m) || !(fabsf(sxy) > m)) return -1;
+    const int c = 4 * ((int)ci + (int)cj * t.nc[0]);
     return c + (dxy < 0.f ? (sxy > 0.f ? 2 : 3) : (sxy > 0.f ? 1 : 0));
 }
 
@@ -261,7 +242,7 @@ static CPAB_HD __noinline__ int cell_3d_exact(float p0, float p1, float p2, cons
 CPAB_HD inline int cell_3d_fast(float p0, float p1, float p2, const Tess &t) {
     // With x and y in [0,1] the push-inside rule does not apply; the
     // reference then clamps each coordinate to [0, clamp3] (in float) and
-    // splits it, which split_cell does exactly.  Only the tetrahedron plane
+    // splits it, which split_exact does exactly.  Only the tetrahedron plane
     // tests need a margin.
     if (!(fabsf(p0) <= 1e30f) || !(fabsf(p1) <= 1e30f) || !(fabsf(p2) <= 1e30f)) return -1;
     if (p0 >= 0.f && p0 <= 1.f && p1 >= 0.f && p1 <= 1.f) {
@@ -269,11 +250,13 @@ CPAB_HD inline int cell_3d_fast(float p0, float p1, float p2, const Tess &t) {
         const float c1 = (p1 < t.clamp3[1]) ? p1 : t.clamp3[1];
         float c2 = (0.f < p2) ? p2 : 0.f;
         c2 = (c2 < t.clamp3[2]) ? c2 : t.clamp3[2];
-        int i, j, k;
-        float r0, r1, r2;
-        split_cell(c0, t.inc[0], t.rinc[0], t.nc[0], i, r0);
-        split_cell(c1, t.inc[1], t.rinc[1], t.nc[1], j, r1);
-        split_cell(c2, t.inc[2], t.rinc[2], t.nc[2], k, r2);
+        float f0, f1, f2, r0, r1, r2;
+        split_exact(c0, t.inc[0], t.rinc[0], f0, r0);
+        split_exact(c1, t.inc[1], t.rinc[1], f1, r1);
+        split_exact(c2, t.inc[2], t.rinc[2], f2, r2);
+        // mymin: the index is capped at nc-1, the remainder is not
+        const int i = min((int)f0, t.nc[0] - 1), j = min((int)f1, t.nc[1] - 1),
+                  k = min((int)f2, t.nc[2] - 1);
         float x = r0 * t.rinc[0], y = r1 * t.rinc[1];
         const float z = r2 * t.rinc[2];
         const bool flip = ((i ^ j ^ k) & 1) != 0;   // the reference's parity rule

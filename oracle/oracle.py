@@ -205,50 +205,104 @@ def _np_round_min(a, b):
     return np.where(a < b, a, np.round(b))
 
 
-def numpy_findcellidx(ndim, p, nc, semantics='numpy'):
-    """Vectorised FP64 cell lookup.
+def _lookup_constants(nc, semantics):
+    """Cell widths and clamps.  'numpy': double 1/nc (libcpab/numpy/findcellidx.py);
+    'cpp': the float values of libcpab/core/cpab_ops.cpp:40-45,108-110,139-141."""
+    ndim = len(nc)
+    if semantics == 'numpy':
+        inc = [1.0 / n for n in nc]
+        width = [nc[j] * inc[j] for j in range(ndim)]
+        clamp = [width[j] - (1e-8) for j in range(ndim)]
+    else:
+        f32 = np.float32
+        inc = [float(f32(1.0 / n)) for n in nc]
+        width = [float(f32(f32(nc[j]) * f32(inc[j]))) for j in range(ndim)]
+        if ndim == 2:
+            clamp = [width[j] - 0.000000001 for j in range(ndim)]
+        else:
+            clamp = [float(f32(width[j] - 1e-8)) for j in range(ndim)]
+            if ndim == 3:   # z clamp with inc_x (cpab_ops.cpp:141)
+                clamp[2] = float(f32(float(f32(f32(nc[2]) * f32(inc[0]))) - 1e-8))
+    return inc, width, clamp
 
-    semantics='numpy': the reference's numpy backend
-    (libcpab/numpy/findcellidx.py:22-150); in 3D it tests z when deciding
-    whether a point is outside.  semantics='cpp': the reference's C++/CUDA
-    rules in 3D (libcpab/core/cpab_ops.cpp:118-141): z is not part of the
-    outside test and z is clamped with nz*inc_x."""
+
+def numpy_findcellidx(ndim, p, nc, semantics='numpy', return_margin=False):
+    """Vectorised FP64 cell lookup of points p [ndim, n].
+
+    semantics='numpy' follows the reference's numpy backend
+    (libcpab/numpy/findcellidx.py:22-150): double cell widths 1/nc, and in 3D
+    z takes part in the outside test.  semantics='cpp' applies the rules of
+    the reference's C++/CUDA lookup (libcpab/core/cpab_ops.cpp:26-184) to
+    double points: float cell widths and clamps, z not tested for the
+    push-inside rule and clamped with nz*inc_x.
+
+    return_margin also returns, per point, the distance (domain units) from
+    the point to the nearest boundary of any decision the lookup takes: cell
+    faces, clamps, sub-cell diagonals / tetrahedron planes, out-of-domain
+    rules and the push-inside comparisons.  A float evaluation can only
+    decide differently when this margin is below its rounding error."""
     p = np.array(p, dtype=np.float64, copy=True)
+    nc = list(nc)
+    inc, width, clamp = _lookup_constants(nc, semantics)
+    big = np.full(p.shape[1], np.inf)
+    margin = big.copy()
     if ndim == 1:
         nx = nc[0]
-        idx = np.floor(p[0] * nx)
-        return np.maximum(0.0, np.minimum(idx, nx - 1)).astype(np.int64)
+        q = p[0] * nx
+        idx = np.maximum(0.0, np.minimum(np.floor(q), nx - 1)).astype(np.int64)
+        if return_margin:
+            margin = np.abs(q - np.round(q)) / nx
+            return idx, margin
+        return idx
     if ndim == 2:
         nx, ny = nc
-        ix, iy = 1.0 / nx, 1.0 / ny
-        p0 = np.minimum(nx * ix - 1e-8, np.maximum(0.0, p[0]))
-        p1 = np.minimum(ny * iy - 1e-8, np.maximum(0.0, p[1]))
+        ix, iy = inc
+        wx, wy = width
+        p0 = np.minimum(clamp[0], np.maximum(0.0, p[0]))
+        p1 = np.minimum(clamp[1], np.maximum(0.0, p[1]))
         xm, ym = np.fmod(p0, ix), np.fmod(p1, iy)
         x, y = xm / ix, ym / iy
-        idx = _np_round_min(nx - 1, (p0 - xm) / ix) + _np_round_min(ny - 1, (p1 - ym) / iy) * nx
-        idx = idx * 4
-        left = p[0] <= 0
-        c1 = left & (p[1] <= 0) & (p[1] / iy < p[0] / ix)
-        c2 = ~c1 & left & (p[1] >= ny * iy) & (p[1] / iy - ny > -p[0] / ix)
+        idx = (_np_round_min(nx - 1, (p0 - xm) / ix) + _np_round_min(ny - 1, (p1 - ym) / iy) * nx) * 4
+        ox, oy = p[0] / ix, p[1] / iy
+        left, right = p[0] <= 0, p[0] >= wx
+        c1 = left & (p[1] <= 0) & (oy < ox)
+        c2 = ~c1 & left & (p[1] >= wy) & (oy - ny > -ox)
         c3 = ~c1 & ~c2 & left
         out = c1 | c2 | c3
-        right = p[0] >= nx * ix
-        c4 = ~out & right & (p[1] <= 0) & (-p[1] / iy > p[0] / ix - nx)
-        c5 = ~out & ~c4 & right & (p[1] >= ny * iy) & (p[1] / iy - ny > p[0] / ix - nx)
+        c4 = ~out & right & (p[1] <= 0) & (-oy > ox - nx)
+        c5 = ~out & ~c4 & right & (p[1] >= wy) & (oy - ny > ox - nx)
         c6 = ~out & ~c4 & ~c5 & right
         out = out | c4 | c5 | c6
-        c7 = ~out & (p[1] >= ny * iy)
+        c7 = ~out & (p[1] >= wy)
         out = out | c7
         c8 = ~out & (x < y) & (1 - x < y)
         c9 = ~out & ~c8 & (x < y)
         c10 = ~out & ~c8 & ~c9 & (x >= y) & (1 - x < y)
         idx = idx + 2 * (c2 | c5 | c7 | c8) + 3 * (c3 | c9) + 1 * (c6 | c10)
+        if return_margin:
+            s = min(ix, iy) / np.sqrt(2)
+            for v in (p[0], p[0] - wx, p[1], p[1] - wy):            # branch tests
+                margin = np.minimum(margin, np.abs(v))
+            inside = ~(left | right | (p[1] <= 0) | (p[1] >= wy))
+            face = np.minimum(np.minimum(xm, ix - xm), np.minimum(ym, iy - ym))
+            tri = np.minimum(np.abs(x - y), np.abs(x + y - 1)) * s
+            margin = np.where(inside, np.minimum(margin, np.minimum(face, tri)), margin)
+            for cond, v in ((left & (p[1] <= 0), oy - ox), (left & (p[1] >= wy), oy - ny + ox),
+                            (right & (p[1] <= 0), -oy - ox + nx),
+                            (right & (p[1] >= wy), oy - ny - ox + nx)):
+                margin = np.where(cond, np.minimum(margin, np.abs(v) * s), margin)
+            # the edge square along the in-range axis
+            margin = np.where(~inside & ~(left | right),
+                              np.minimum(margin, np.minimum(xm, ix - xm)), margin)
+            margin = np.where(~inside & (left | right) & (p[1] > 0) & (p[1] < wy),
+                              np.minimum(margin, np.minimum(ym, iy - ym)), margin)
+            return idx.astype(np.int64), margin
         return idx.astype(np.int64)
     nx, ny, nz = nc
+    ix, iy, iz = inc
     outside = (p[0] < 0) | (p[0] > 1) | (p[1] < 0) | (p[1] > 1)
     if semantics == 'numpy':
         outside = outside | (p[2] < 0) | (p[2] > 1)
-    ix, iy, iz = 1.0 / nx, 1.0 / ny, 1.0 / nz
     h = 0.5
     q = p[:, outside] - h
     a = np.abs(q)
@@ -258,24 +312,40 @@ def numpy_findcellidx(ndim, p, nc, semantics='numpy'):
     for j in range(3):
         m = a[j] > h
         q[j, m] = np.copysign(h - push[j][m], q[j, m])
-    p[:, outside] = q + h
-    p0 = np.minimum(nx * ix - 1e-8, np.maximum(0.0, p[0]))
-    p1 = np.minimum(ny * iy - 1e-8, np.maximum(0.0, p[1]))
-    p2 = np.minimum(nz * (iz if semantics == 'numpy' else ix) - 1e-8, np.maximum(0.0, p[2]))
-    xm, ym, zm = np.mod(p0, ix), np.mod(p1, iy), np.mod(p2, iz)
-    i = _np_round_min(nx - 1, (p0 - xm) / ix)
-    j = _np_round_min(ny - 1, (p1 - ym) / iy)
-    k = _np_round_min(nz - 1, (p2 - zm) / iz)
-    idx = 5 * (i + j * nx + k * nx * ny)
-    x, y, z = xm / ix, ym / iy, zm / iz
-    flip = (((k % 2 == 0) & (i % 2 == 0) & (j % 2 == 1)) | ((k % 2 == 0) & (i % 2 == 1) & (j % 2 == 0)) |
-            ((k % 2 == 1) & (i % 2 == 0) & (j % 2 == 0)) | ((k % 2 == 1) & (i % 2 == 1) & (j % 2 == 1)))
+    pp = p.copy()
+    pp[:, outside] = q + h
+    c = [np.minimum(clamp[j], np.maximum(0.0, pp[j])) for j in range(3)]
+    xm = [np.mod(c[j], inc[j]) for j in range(3)]
+    i = _np_round_min(nx - 1, (c[0] - xm[0]) / ix)
+    j_ = _np_round_min(ny - 1, (c[1] - xm[1]) / iy)
+    k = _np_round_min(nz - 1, (c[2] - xm[2]) / iz)
+    idx = 5 * (i + j_ * nx + k * nx * ny)
+    x, y, z = xm[0] / ix, xm[1] / iy, xm[2] / iz
+    flip = (((k % 2 == 0) & (i % 2 == 0) & (j_ % 2 == 1)) | ((k % 2 == 0) & (i % 2 == 1) & (j_ % 2 == 0)) |
+            ((k % 2 == 1) & (i % 2 == 0) & (j_ % 2 == 0)) | ((k % 2 == 1) & (i % 2 == 1) & (j_ % 2 == 1)))
     x, y = np.where(flip, y, x), np.where(flip, 1 - x, y)
     t1 = -x - y + z >= 0
     t2 = x + y + z - 2 >= 0
     t3 = -x + y - z >= 0
     t4 = x - y - z >= 0
     idx = idx + 1 * t1 + 2 * (t2 & ~t1) + 3 * (t3 & ~t1 & ~t2) + 4 * (t4 & ~t1 & ~t2 & ~t3)
+    if return_margin:
+        s = min(inc) / np.sqrt(3)
+        for v in (p[0], p[0] - 1, p[1], p[1] - 1):                 # push-inside test
+            margin = np.minimum(margin, np.abs(v))
+        pm = np.full(p.shape[1], np.inf)                          # push comparisons
+        for u, v in ((0, 1), (0, 2), (1, 2)):
+            pm[outside] = np.minimum(pm[outside], np.abs(a[u] - a[v]))
+        for j in range(3):
+            pm[outside] = np.minimum(pm[outside], np.abs(a[j] - h))
+        margin = np.minimum(margin, pm)
+        for j in range(3):
+            margin = np.minimum(margin, np.abs(pp[j] - clamp[j]))
+            margin = np.minimum(margin, np.where(pp[j] > 0, np.abs(pp[j]), np.inf))
+            margin = np.minimum(margin, np.minimum(xm[j], inc[j] - xm[j]))
+        for v in (-x - y + z, x + y + z - 2, -x + y - z, x - y - z):
+            margin = np.minimum(margin, np.abs(v) * s)
+        return idx.astype(np.int64), margin
     return idx.astype(np.int64)
 
 
@@ -291,40 +361,6 @@ def step_maps_fp64(basis, theta, ndim, nsteps):
     dT = 1.0 / nsteps
     T = np.stack([expm(dT * a) for a in Asq])
     return T.reshape(n_theta, nC, ndim + 1, ndim + 1)
-
-
-def decision_margin(ndim, p, nc):
-    """Distance (domain units) from each point p [ndim, n] to the nearest
-    boundary that the cell lookup decides on: cell faces, the triangle
-    diagonals (2D), the tetrahedron planes (3D) and the out-of-domain rules.
-    An fp32 trajectory can only take a different cell than the FP64 one at a
-    step whose margin is below its rounding drift (a boundary tie)."""
-    p = np.asarray(p, dtype=np.float64)
-    inc = [1.0 / n for n in nc]
-    m = np.full(p.shape[1], np.inf)
-    for j in range(ndim):
-        q = p[j] / inc[j]
-        m = np.minimum(m, np.abs(q - np.round(q)) * inc[j])
-    if ndim == 1:
-        return m
-    fr = [np.mod(np.clip(p[j], 0, 1 - 1e-12), inc[j]) / inc[j] for j in range(ndim)]
-    if ndim == 2:
-        x, y = fr
-        s = min(inc) / np.sqrt(2)
-        m = np.minimum(m, np.abs(x - y) * s)
-        m = np.minimum(m, np.abs(x + y - 1) * s)
-        # out-of-domain diagonal rules (cpab_ops.cpp:57-79)
-        ox, oy = p[0] / inc[0], p[1] / inc[1]
-        out = (p[0] <= 0) | (p[0] >= 1) | (p[1] <= 0) | (p[1] >= 1)
-        for diff in (oy - ox, oy - nc[1] + ox, -oy - ox + nc[0], oy - nc[1] - ox + nc[0]):
-            m = np.where(out, np.minimum(m, np.abs(diff) * s), m)
-        return m
-    x, y, z = fr
-    s = min(inc) / np.sqrt(3)
-    for xx, yy in ((x, y), (y, 1 - x)):
-        for v in (-xx - yy + z, xx + yy + z - 2, -xx + yy - z, xx - yy - z):
-            m = np.minimum(m, np.abs(v) * s)
-    return m
 
 
 def numpy_transform_grid(basis, theta, points, nc, nsteps=50, return_cells=False,
@@ -349,9 +385,11 @@ def numpy_transform_grid(basis, theta, points, nc, nsteps=50, return_cells=False
     base = np.repeat(np.arange(n_theta) * nC, nP)
     cells, margins = [], []
     for _ in range(nsteps):
-        c = numpy_findcellidx(ndim, Ph[:, :ndim, 0].T, nc, semantics)
         if return_margin:
-            margins.append(decision_margin(ndim, Ph[:, :ndim, 0].T, nc))
+            c, mg = numpy_findcellidx(ndim, Ph[:, :ndim, 0].T, nc, semantics, return_margin=True)
+            margins.append(mg)
+        else:
+            c = numpy_findcellidx(ndim, Ph[:, :ndim, 0].T, nc, semantics)
         cells.append(c)
         Ph = np.matmul(Tf[c + base], Ph)
     out = Ph[:, :ndim, 0].reshape(n_theta, nP, ndim).transpose(0, 2, 1)

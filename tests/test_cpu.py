@@ -73,6 +73,22 @@ def test_oracle_cell_lookup_matches_reference(name, oracle):
     assert np.array_equal(numpy_findcellidx(len(nc), g['probe'], nc), g['cells_np'])
 
 
+@pytest.mark.parametrize('nc', [[50], [3, 3], [8, 8], [2, 2, 2], [4, 4, 4], [3, 5, 2]])
+def test_fp64_cpp_lookup_matches_oracle_except_ties(nc, oracle):
+    """The FP64 lookup with the C++ rules (used to follow trajectories in
+    double) gives the C oracle's cell for float inputs, except at points whose
+    decision margin marks them as ties."""
+    from oracle.oracle import numpy_findcellidx
+    rng = np.random.default_rng(11)
+    P = rng.uniform(-0.5, 1.5, (len(nc), 300000)).astype(np.float32)
+    P[:, :100000] = rng.uniform(0, 1, (len(nc), 100000))
+    got, margin = numpy_findcellidx(len(nc), P, nc, semantics='cpp', return_margin=True)
+    ref = oracle.findcellidx(nc, P)
+    bad = got != ref
+    assert np.all(margin[bad] < 1e-6), margin[bad].max()
+    assert bad.mean() < 1e-3
+
+
 @pytest.mark.parametrize('name', SMALL)
 def test_oracle_forward_matches_reference(name, oracle):
     """C restatement fed the reference's step maps: bit-identical to the

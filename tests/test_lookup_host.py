@@ -75,6 +75,20 @@ def adversarial(nc, rng, n=400000):
     val = rng.choice(np.array([0.0, -0.0, 1e-30, 1e-12, -1e-12, 1.0, np.nextafter(np.float32(1), np.float32(0))],
                               dtype=np.float32), m)
     P[face, i1 + np.arange(m)] = val
+    # far outside, huge and non-finite coordinates
+    i2 = i1 + m
+    P[:, i2:i2 + m] = rng.uniform(-6, 7, (ndim, m)).astype(np.float32)
+    spec = np.array([np.nan, np.inf, -np.inf, 1e10, -1e10, 3e38, 1e-38], dtype=np.float32)
+    k = i2 + rng.choice(m, m // 20, replace=False)
+    P[rng.integers(0, ndim, k.size), k] = rng.choice(spec, k.size)
+    # out-of-domain diagonal rules: |py/iy| == |px/ix| corners, to the ulp
+    if ndim == 2:
+        i3 = i2 + m // 2
+        s = rng.uniform(0.01, 2, m // 2)
+        sx = rng.choice([-1, 1], m // 2)
+        sy = rng.choice([-1, 1], m // 2)
+        P[0, i3:i2 + m] = np.where(sx < 0, -s / nc[0], 1 + s / nc[0]).astype(np.float32)
+        P[1, i3:i2 + m] = np.where(sy < 0, -s / nc[1], 1 + s / nc[1]).astype(np.float32)
     return P
 
 
