@@ -56,7 +56,8 @@ __global__ void __launch_bounds__(256)
     float *tab = reinterpret_cast<float *>(smem4);
     float *gw = tab + Gr;
     float *ck = gw + (size_t)W * Gr;
-    CT *cl = reinterpret_cast<CT *>(ck + (size_t)nseg * N * B);
+    float *pb = ck + (size_t)nseg * N * B;
+    CT *cl = reinterpret_cast<CT *>(pb + (size_t)kSeg * N * B);
 
     const int th = blockIdx.x / parts, part = blockIdx.x % parts;
     if (!stage_table(tab, table + (long long)th * G, G, &bar, err)) return;
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(256)
         logged_forward<N, MODE, CT>(tab, t, nsteps, st, p, ck, cl, ties, err);
 #pragma unroll
         for (int r = 0; r < N; ++r) lam[r] = live ? __ldg(gout + ((long long)th * N + r) * nP + idx) : 0.f;
-        reverse_sweep<N, MODE, CT>(tab, ck, cl, nsteps, st, live, lam, warp_tab);
+        reverse_sweep<N, MODE, CT>(tab, ck, cl, pb, nsteps, st, live, lam, warp_tab);
         if (dpoints && live) {
 #pragma unroll
             for (int r = 0; r < N; ++r) dpoints[((long long)th * N + r) * nP + idx] = lam[r];

@@ -127,25 +127,31 @@ __host__ __device__ inline int round4(int x) { return (x + 3) & ~3; }
 // Shared memory carve-up for the adjoint kernels (floats unless noted):
 //   tab   [round4(G)]            cell table of this theta (TMA destination)
 //   gw    [W][round4(G)]         per-warp cell-gradient tables
-//   ck    [nseg][N][block]       checkpoints
+//   ck    [nseg][N][block]       checkpoints (position every kSeg steps)
+//   pb    [kSeg][N][block]       positions of the segment being reversed
 //   cl    [nsteps][block] (CT)   per-step cells
+// Every array is indexed [...][block] by thread, so warps access
+// consecutive words (no bank conflicts).
 template <int N, typename CT>
 __host__ __device__ inline size_t adjoint_smem_bytes(int nC, int nsteps, int block) {
     const int G = round4(nC * N * (N + 1));
     const int W = block / 32;
     const int nseg = (nsteps + kSeg - 1) / kSeg;
     size_t b = (size_t)G * 4 + (size_t)W * G * 4 + (size_t)nseg * N * block * 4 +
-               (size_t)nsteps * block * sizeof(CT);
+               (size_t)kSeg * N * block * 4 + (size_t)nsteps * block * sizeof(CT);
     return (b + 15) & ~(size_t)15;
 }
 
 // Reverse sweep of one trajectory whose cells are logged in cl and whose
 // checkpoints are in ck; lam holds dL/dp_N on entry and dL/dp_0 on exit.
+// Each segment's positions are rebuilt from its checkpoint with the logged
+// cells (no lookups) into pb, then walked backwards.  The loops are not
+// unrolled: the body stays small enough for the instruction cache.
 // Executed by all lanes of the warp (uniform trip counts).
 template <int N, int MODE, typename CT>
 __device__ __forceinline__ void reverse_sweep(const float *tab, const float *ck, const CT *cl,
-                                              int nsteps, const Steps &st, bool live,
-                                              float (&lam)[N], float *warp_tab) {
+                                              float *pb, int nsteps, const Steps &st,
+                                              bool live, float (&lam)[N], float *warp_tab) {
     constexpr int P = N * (N + 1);
     const int B = blockDim.x, tid = threadIdx.x;
     const int nseg = (nsteps + kSeg - 1) / kSeg;
@@ -155,34 +161,34 @@ __device__ __forceinline__ void reverse_sweep(const float *tab, const float *ck,
     int gcell = -1;
     for (int seg = nseg - 1; seg >= 0; --seg) {
         const int n0 = seg * kSeg;
-        float q[N], pb[kSeg][N];
+        const int len = min(kSeg, nsteps - n0);
+        float q[N];
 #pragma unroll
         for (int r = 0; r < N; ++r) q[r] = ck[(seg * N + r) * B + tid];
+#pragma unroll 1
+        for (int s = 0; s < len; ++s) {
 #pragma unroll
-        for (int s = 0; s < kSeg; ++s) {
-            if (n0 + s < nsteps) {
-#pragma unroll
-                for (int r = 0; r < N; ++r) pb[s][r] = q[r];
-                traj_step<N, MODE>(tab, (int)cl[(n0 + s) * B + tid], st, q);
-            }
+            for (int r = 0; r < N; ++r) pb[(s * N + r) * B + tid] = q[r];
+            traj_step<N, MODE>(tab, (int)cl[(n0 + s) * B + tid], st, q);
         }
-#pragma unroll
-        for (int s = kSeg - 1; s >= 0; --s) {
-            if (n0 + s < nsteps) {
-                const int c = (int)cl[(n0 + s) * B + tid];
-                const bool change = c != gcell;
-                const unsigned m = __ballot_sync(0xffffffffu, change && gcell >= 0 && live);
-                if (m) {
-                    if ((m >> (tid & 31)) & 1u) flush_group<P>(m, gcell, acc, warp_tab);
-                    __syncwarp();
-                }
-                if (change) {
-                    gcell = c;
-#pragma unroll
-                    for (int i = 0; i < P; ++i) acc[i] = 0.f;
-                }
-                adjoint_step<N, MODE>(tab, c, st, pb[s], lam, acc);
+#pragma unroll 1
+        for (int s = len - 1; s >= 0; --s) {
+            const int c = (int)cl[(n0 + s) * B + tid];
+            const bool change = c != gcell;
+            const unsigned m = __ballot_sync(0xffffffffu, change && gcell >= 0 && live);
+            if (m) {
+                if ((m >> (tid & 31)) & 1u) flush_group<P>(m, gcell, acc, warp_tab);
+                __syncwarp();
             }
+            if (change) {
+                gcell = c;
+#pragma unroll
+                for (int i = 0; i < P; ++i) acc[i] = 0.f;
+            }
+            float p[N];
+#pragma unroll
+            for (int r = 0; r < N; ++r) p[r] = pb[(s * N + r) * B + tid];
+            adjoint_step<N, MODE>(tab, c, st, p, lam, acc);
         }
     }
     const unsigned m = __ballot_sync(0xffffffffu, gcell >= 0 && live);

@@ -29,6 +29,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 namespace cpab {
 
@@ -53,6 +54,7 @@ struct Tess {
     float wlim[3];    // (float)nc * inc     (float product)
     float clamp3[3];  // 3D clamp limits (float)(nc*inc - 1e-8), z uses inc_x
     int band[3];      // 1 if (float)(nc*inc) > nc*inc: floats in [nc*inc, wlim) exist
+    float ncf[3];     // nc as float
 };
 
 // The lookup functions are host+device so that a host harness can check the
@@ -83,6 +85,7 @@ inline int tess_init(int ndim, const int *nc, Tess *t) {
         t->rinc[j] = (float)(1.0 / (double)t->inc[j]);
         t->wlim[j] = (float)n * t->inc[j];
         t->band[j] = (double)t->wlim[j] > (double)n * (double)t->inc[j];
+        t->ncf[j] = (float)n;
         cells *= n;
     }
     t->nC = (int)(cells * (ndim == 1 ? 1 : ndim == 2 ? 4 : 5));
@@ -96,14 +99,43 @@ inline int tess_init(int ndim, const int *nc, Tess *t) {
 
 CPAB_HD inline int mymin_ref(int a, double b) { return !(b < a) ? a : (int)round(b); }
 
+// Rounding and float->int without conversion instructions (on GB300 these
+// issue to the narrow FP64 pipe and throttled the lookup): adding 1.5*2^23
+// rounds |x| < 2^22 to the nearest integer and leaves it in the low
+// mantissa bits.
+constexpr float kRoundMagic = 12582912.0f;      // 1.5 * 2^23
+constexpr int kRoundMagicBits = 0x4B400000;     // bit pattern of kRoundMagic
+
+CPAB_HD inline int float_bits(float x) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_int(x);
+#else
+    int i;
+    memcpy(&i, &x, sizeof(i));
+    return i;
+#endif
+}
+
+// Nearest integer (ties to even) of |x| < 2^22.
+CPAB_HD inline float round_small(float x) {
+    return CPAB_SUB_RN(CPAB_ADD_RN(x, kRoundMagic), kRoundMagic);
+}
+
+// int value of an integral float with |x| < 2^22.
+CPAB_HD inline int small_float_to_int(float x) {
+    return float_bits(CPAB_ADD_RN(x, kRoundMagic)) - kRoundMagicBits;
+}
+
 // ------------------------------- 1D ---------------------------------------
-// Exact in FP32: floor(p * nc) with the float product, clamped
-// (cpab_ops.cu:14-19).
+// floor(p * nc) with the float product, clamped to [0, nc-1]
+// (cpab_ops.cu:14-19).  Non-finite and huge products saturate like CUDA's
+// float->int conversion: +inf and large values give nc-1, -inf and NaN give 0.
 CPAB_HD inline int cell_1d(float p, const Tess &t) {
-    float q = floorf(CPAB_MUL_RN(p, (float)t.nc[0]));
-    int idx = (int)q;
-    idx = max(0, min(idx, t.nc[0] - 1));
-    return idx;
+    const float q = CPAB_MUL_RN(p, t.ncf[0]);
+    const float k = round_small(q);
+    float f = (k > q) ? k - 1.f : k;                    // floor, exact for |q| < 2^22
+    f = fminf(fmaxf(f, 0.f), t.ncf[0] - 1.f);          // NaN -> 0
+    return small_float_to_int(f);
 }
 
 // ------------------------------- 2D ---------------------------------------
@@ -144,10 +176,13 @@ static CPAB_HD __noinline__ int cell_2d_exact(float fpx, float fpy, const Tess &
 // inc's ulp grid, so the second fma returns it exactly: these are the
 // reference's fmod/divide results (cpab_ops.cpp:47-54) without FP64.
 CPAB_HD inline void split_exact(float p, float inc, float rinc, float &fi, float &rem) {
-    const float k = rintf(p * rinc);
+    const float k = round_small(p * rinc);
     fi = (fmaf(-k, inc, p) >= 0.f) ? k : k - 1.f;
     rem = fmaf(-fi, inc, p);
 }
+
+// |p * rinc| below this keeps every integer in split_exact exact.
+constexpr float kSplitLimit = 2097152.0f;   // 2^21
 
 // Margin of the FP32 sub-cell tests.  A sub-cell coordinate rem*rinc differs
 // from the reference's double rem/inc by at most 2^-22; a two-term test then
@@ -170,8 +205,11 @@ CPAB_HD inline int cell_2d_fast(float px, float py, const Tess &t) {
     float fi, ri, fj, rj;
     split_exact(px, t.inc[0], t.rinc[0], fi, ri);
     split_exact(py, t.inc[1], t.rinc[1], fj, rj);
-    const float ci = fminf(fmaxf(fi, 0.f), (float)(t.nc[0] - 1));
-    const float cj = fminf(fmaxf(fj, 0.f), (float)(t.nc[1] - 1));
+    // far away, huge or non-finite coordinates: FP64 replica
+    if (!(fabsf(px * t.rinc[0]) < kSplitLimit) || !(fabsf(py * t.rinc[1]) < kSplitLimit))
+        return -1;
+    const float ci = fminf(fmaxf(fi, 0.f), t.ncf[0] - 1.f);
+    const float cj = fminf(fmaxf(fj, 0.f), t.ncf[1] - 1.f);
     // In-domain points past nc*inc (possible only when the float product
     // nc*inc rounds above it) get the fmod remainder, not the continuous one.
     if ((t.band[0] && fi > ci && px < t.wlim[0]) || (t.band[1] && fj > cj && py < t.wlim[1]))
@@ -181,8 +219,8 @@ CPAB_HD inline int cell_2d_fast(float px, float py, const Tess &t) {
     const float dxy = x - y, sxy = (x + y) - 1.f;
     const float m = kMargin2 * ((1.f + fabsf(x)) + fabsf(y));
     if (!(fabsf(dxy) > m) || !(fabsf(sxy) > m)) return -1;
-    const int c = 4 * ((int)ci + (int)cj * t.nc[0]);
-    return c + (dxy < 0.f ? (sxy > 0.f ? 2 : 3) : (sxy > 0.f ? 1 : 0));
+    const float tri = dxy < 0.f ? (sxy > 0.f ? 2.f : 3.f) : (sxy > 0.f ? 1.f : 0.f);
+    return small_float_to_int(fmaf(4.f, fmaf(cj, t.ncf[0], ci), tri));
 }
 
 __device__ __forceinline__ int cell_2d(float px, float py, const Tess &t,
@@ -255,8 +293,9 @@ CPAB_HD inline int cell_3d_fast(float p0, float p1, float p2, const Tess &t) {
         split_exact(c1, t.inc[1], t.rinc[1], f1, r1);
         split_exact(c2, t.inc[2], t.rinc[2], f2, r2);
         // mymin: the index is capped at nc-1, the remainder is not
-        const int i = min((int)f0, t.nc[0] - 1), j = min((int)f1, t.nc[1] - 1),
-                  k = min((int)f2, t.nc[2] - 1);
+        const int i = small_float_to_int(fminf(f0, t.ncf[0] - 1.f));
+        const int j = small_float_to_int(fminf(f1, t.ncf[1] - 1.f));
+        const int k = small_float_to_int(fminf(f2, t.ncf[2] - 1.f));
         float x = r0 * t.rinc[0], y = r1 * t.rinc[1];
         const float z = r2 * t.rinc[2];
         const bool flip = ((i ^ j ^ k) & 1) != 0;   // the reference's parity rule

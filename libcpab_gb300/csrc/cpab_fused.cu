@@ -145,7 +145,8 @@ __global__ void __launch_bounds__(256)
     float *tab = reinterpret_cast<float *>(smem4);
     float *gw = tab + Gr;
     float *ck = gw + (size_t)W * Gr;
-    CT *cl = reinterpret_cast<CT *>(ck + (size_t)nseg * N * B);
+    float *pb = ck + (size_t)nseg * N * B;
+    CT *cl = reinterpret_cast<CT *>(pb + (size_t)kSeg * N * B);
 
     const int b = blockIdx.x / parts, part = blockIdx.x % parts;
     if (!stage_table(tab, table + (long long)b * G, G, &bar, err)) return;
@@ -182,7 +183,7 @@ __global__ void __launch_bounds__(256)
         }
 #pragma unroll
         for (int r = 0; r < N; ++r) lam[r] = gf[r] * (float)(g.size[r] - 1);
-        reverse_sweep<N, MODE, CT>(tab, ck, cl, nsteps, st, live, lam, warp_tab);
+        reverse_sweep<N, MODE, CT>(tab, ck, cl, pb, nsteps, st, live, lam, warp_tab);
     }
     __syncthreads();
     float *dst = partials + ((long long)b * parts + part) * G;

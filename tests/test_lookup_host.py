@@ -99,6 +99,13 @@ def test_fp32_lookup_agrees_with_fp64_replica_and_oracle(nc, harness, tmp_path, 
     P = adversarial(nc, rng)
     fast, exact = run(harness, tmp_path, nc, P)
     ref = oracle.findcellidx(nc, P)
+    if len(nc) == 1:
+        # floor(p*nc) of a huge or non-finite p has no defined int value in C;
+        # the kernels saturate like CUDA's conversion (see cell_1d)
+        ok = np.abs(P[0]) < 1e6
+        sat = np.where(np.isnan(P[0]) | (P[0] < 0), 0, nc[0] - 1)
+        assert np.array_equal(exact[~ok], sat[~ok])
+        exact, ref, fast, P = exact[ok], ref[ok], fast[ok], P[:, ok]
     assert np.array_equal(exact, ref), 'FP64 replica differs from the oracle'
     answered = fast >= 0
     bad = np.nonzero(answered & (fast != exact))[0]
