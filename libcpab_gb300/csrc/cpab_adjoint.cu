@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(256)
     float *pb = ck + (size_t)nseg * N * B;
     CT *cl = reinterpret_cast<CT *>(pb + (size_t)kSeg * N * B);
 
-    const int th = blockIdx.x / parts, part = blockIdx.x % parts;
+    const int th = blockIdx.y, part = blockIdx.x;
     if (!stage_table(tab, table + (long long)th * G, G, &bar, err)) return;
     for (int i = tid; i < W * Gr; i += B) gw[i] = 0.f;
     __syncthreads();
@@ -161,9 +161,10 @@ static cudaError_t launch_adjoint_t(const Tess &t, int nsteps, const AdjointPlan
     st.h = (float)(1.0 / nsteps);
     st.hh = (float)(0.5 / nsteps);
     st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
-    const long long grid = (long long)n_theta * plan.parts;
-    if (grid == 0) return cudaSuccess;
-    kern<<<(unsigned)grid, plan.block, plan.smem, s>>>(t, nsteps, st, points, broadcast, nP, table,
+    if (n_theta == 0) return cudaSuccess;
+    if (n_theta > 65535) return cudaErrorInvalidConfiguration;   // theta on grid y
+    const dim3 grid((unsigned)plan.parts, (unsigned)n_theta);
+    kern<<<grid, plan.block, plan.smem, s>>>(t, nsteps, st, points, broadcast, nP, table,
                                                        plan.parts, plan.tiles, gout, dpoints,
                                                        partials, ties, err);
     return cudaGetLastError();

@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include "../../include/cpab_gb300.h"
+#include "cpab_interp.cuh"
 #include "cpab_launch.h"
 
 using namespace cpab;
@@ -76,6 +77,25 @@ int check_sizes(int ndim, const int *v, const char *name) {
     return CPAB_OK;
 }
 
+// Image geometry: positive extents, per-image sizes within the kernels'
+// 32-bit indexing, and at most 65535 images (one grid row each, as the
+// reference's launches put the batch on the grid's y dimension).
+int check_geo(int ndim, const int *size, const int *outsize, int nb) {
+    int rc;
+    if ((rc = check_sizes(ndim, size, "size")) || (rc = check_sizes(ndim, outsize, "outsize")))
+        return rc;
+    if (!geo_fits(ndim, size, outsize))
+        return fail(CPAB_ERR_UNSUPPORTED, "image too large (per-image elements must be < 2^31)");
+    if (nb > 65535) return fail(CPAB_ERR_UNSUPPORTED, "at most 65535 images per call (got %d)", nb);
+    return CPAB_OK;
+}
+
+int check_theta_count(int n_theta) {
+    if (n_theta > 65535)
+        return fail(CPAB_ERR_UNSUPPORTED, "at most 65535 transformations per call (got %d)", n_theta);
+    return CPAB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -114,6 +134,7 @@ static int integrate_common(int ndim, const int *nc, int nsteps, const float *po
     if (rc) return rc;
     if ((rc = check_steps(nsteps))) return rc;
     if (nP < 0 || n_theta < 0) return fail(CPAB_ERR_ARGUMENT, "negative size");
+    if ((rc = check_theta_count(n_theta))) return rc;
     if (nP == 0 || n_theta == 0) return CPAB_OK;
     if (!points || !table || !out) return fail(CPAB_ERR_ARGUMENT, "points, table or out is NULL");
     unsigned *err = device_error_word();
@@ -169,6 +190,7 @@ int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *po
     if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
         return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
     if (nP < 0 || n_theta < 0 || d < 0) return fail(CPAB_ERR_ARGUMENT, "invalid sizes");
+    if ((rc = check_theta_count(n_theta))) return rc;
     if (n_theta == 0 || (d == 0 && !dpoints)) return CPAB_OK;   // nothing to compute
     if (!A || (d > 0 && (!dtheta || !basis)))
         return fail(CPAB_ERR_ARGUMENT, "dtheta, basis or A is NULL");
@@ -202,7 +224,7 @@ int cpab_interpolate(int ndim, const float *data, int nb, int C, const int *size
     g_err[0] = 0;
     if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3");
     int rc;
-    if ((rc = check_sizes(ndim, size, "size")) || (rc = check_sizes(ndim, outsize, "outsize")))
+    if ((rc = check_geo(ndim, size, outsize, nb)))
         return rc;
     if (nb < 0 || C < 1) return fail(CPAB_ERR_ARGUMENT, "invalid nb or C");
     if (nb == 0) return CPAB_OK;
@@ -217,7 +239,7 @@ int cpab_interpolate_backward(int ndim, const float *data, int nb, int C, const 
     g_err[0] = 0;
     if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3");
     int rc;
-    if ((rc = check_sizes(ndim, size, "size")) || (rc = check_sizes(ndim, outsize, "outsize")))
+    if ((rc = check_geo(ndim, size, outsize, nb)))
         return rc;
     if (nb < 0 || C < 1) return fail(CPAB_ERR_ARGUMENT, "invalid nb or C");
     if (nb == 0) return CPAB_OK;
@@ -243,7 +265,7 @@ int cpab_transform_data(int ndim, const int *nc, int nsteps, const float *lin,
     int rc = make_tess(ndim, nc, &t);
     if (rc) return rc;
     if ((rc = check_steps(nsteps))) return rc;
-    if ((rc = check_sizes(ndim, size, "size")) || (rc = check_sizes(ndim, outsize, "outsize")))
+    if ((rc = check_geo(ndim, size, outsize, nb)))
         return rc;
     if (nb < 0 || C < 1) return fail(CPAB_ERR_ARGUMENT, "invalid nb or C");
     if (nb == 0) return CPAB_OK;
@@ -282,7 +304,7 @@ int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, int mode,
     int rc = make_tess(ndim, nc, &t);
     if (rc) return rc;
     if ((rc = check_steps(nsteps))) return rc;
-    if ((rc = check_sizes(ndim, size, "size")) || (rc = check_sizes(ndim, outsize, "outsize")))
+    if ((rc = check_geo(ndim, size, outsize, nb)))
         return rc;
     if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
         return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);

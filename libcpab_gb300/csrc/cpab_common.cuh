@@ -126,6 +126,37 @@ CPAB_HD inline int small_float_to_int(float x) {
     return float_bits(CPAB_ADD_RN(x, kRoundMagic)) - kRoundMagicBits;
 }
 
+// Division of 32-bit unsigned numerators by a fixed divisor d >= 1 with one
+// multiply-high (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994): m = floor(2^32 (2^l - d) / d) + 1 with
+// l = ceil(log2 d); q = (hi + ((n - hi) >> 1)) >> (l - 1), hi = mulhi(n, m).
+// Exact for every 32-bit n; avoids the int<->float conversions of the
+// generic division sequence.
+struct FastDiv {
+    unsigned d, m;
+    int s;   // l - 1, or -1 for d == 1
+};
+
+inline FastDiv make_fastdiv(unsigned d) {
+    FastDiv f;
+    f.d = d;
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    f.m = (unsigned)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    f.s = l - 1;
+    return f;
+}
+
+CPAB_HD inline unsigned fast_div(unsigned n, const FastDiv &f) {
+    if (f.s < 0) return n;
+#if defined(__CUDA_ARCH__)
+    const unsigned hi = __umulhi(n, f.m);
+#else
+    const unsigned hi = (unsigned)(((unsigned long long)n * f.m) >> 32);
+#endif
+    return (hi + ((n - hi) >> 1)) >> f.s;
+}
+
 // ------------------------------- 1D ---------------------------------------
 // floor(p * nc) with the float product, clamped to [0, nc-1]
 // (cpab_ops.cu:14-19).  Non-finite and huge products saturate like CUDA's

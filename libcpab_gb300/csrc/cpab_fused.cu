@@ -24,14 +24,14 @@ namespace cpab {
 
 // Axis indices of output element o (last axis fastest) and its grid point.
 template <int N>
-__device__ __forceinline__ void grid_point(long long o, const Geo &g, const float *lin,
-                                           float (&p)[N]) {
-    long long idx[N];
-    long long r = o;
+__device__ __forceinline__ void grid_point(int o, const Geo &g, const float *lin, float (&p)[N]) {
+    unsigned idx[N];
+    unsigned r = (unsigned)o;
 #pragma unroll
     for (int j = N - 1; j >= 0; --j) {
-        idx[j] = r % g.outsize[j];
-        r /= g.outsize[j];
+        const unsigned q = fast_div(r, g.dout[j]);
+        idx[j] = r - q * g.outsize[j];
+        r = q;
     }
     int off = 0;
 #pragma unroll
@@ -51,14 +51,14 @@ __global__ void __launch_bounds__(256)
     extern __shared__ float4 smem4[];
     __shared__ uint64_t bar;
     float *tab = reinterpret_cast<float *>(smem4);
-    const int b = blockIdx.x / tiles, tile = blockIdx.x % tiles;
+    const int b = blockIdx.y, tile = blockIdx.x;
     const int G = t.nC * P;
     if (!stage_table(tab, E + (long long)b * G, G, &bar, err)) return;
     float p[PPT][N];
-    long long o[PPT];
+    int o[PPT];
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
-        o[j] = ((long long)tile * PPT + j) * blockDim.x + threadIdx.x;
+        o[j] = (tile * PPT + j) * (int)blockDim.x + (int)threadIdx.x;
         if (o[j] < g.nP) grid_point<N>(o[j], g, lin, p[j]);
         else {
 #pragma unroll
@@ -105,8 +105,8 @@ cudaError_t launch_transform_data(const Tess &t, int nsteps, const float *lin, c
     const int ppt = two ? 2 : 1;
     const long long per = (long long)block * ppt;
     const int tiles = (int)((g.nP + per - 1) / per);
-    const long long grid = (long long)tiles * nb;
-    if (grid > 0x7fffffffll) return cudaErrorInvalidConfiguration;
+    if (nb > 65535) return cudaErrorInvalidConfiguration;   // images on grid y
+    const dim3 grid((unsigned)tiles, (unsigned)nb);
     const size_t smem = (size_t)t.nC * t.ndim * (t.ndim + 1) * sizeof(float);
 #define CPAB_TD(N, PP)                                                                         \
     {                                                                                          \
@@ -116,7 +116,7 @@ cudaError_t launch_transform_data(const Tess &t, int nsteps, const float *lin, c
                 kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                 \
             if (e != cudaSuccess) return e;                                                    \
         }                                                                                      \
-        kern<<<(unsigned)grid, block, smem, s>>>(t, nsteps, g, lin, E, C, data, out, grid_out, \
+        kern<<<grid, block, smem, s>>>(t, nsteps, g, lin, E, C, data, out, grid_out, \
                                                  tiles, ties, err);                            \
         return cudaGetLastError();                                                             \
     }
@@ -148,14 +148,14 @@ __global__ void __launch_bounds__(256)
     float *pb = ck + (size_t)nseg * N * B;
     CT *cl = reinterpret_cast<CT *>(pb + (size_t)kSeg * N * B);
 
-    const int b = blockIdx.x / parts, part = blockIdx.x % parts;
+    const int b = blockIdx.y, part = blockIdx.x;
     if (!stage_table(tab, table + (long long)b * G, G, &bar, err)) return;
     for (int i = tid; i < W * Gr; i += B) gw[i] = 0.f;
     __syncthreads();
     float *warp_tab = gw + (size_t)(tid >> 5) * Gr;
 
     for (int tile = part; tile < tiles; tile += parts) {
-        const long long o = (long long)tile * B + tid;
+        const int o = tile * B + tid;
         const bool live = o < g.nP;
         float p[N], pN[N], lam[N];
         if (live) grid_point<N>(o, g, lin, p);
@@ -258,9 +258,10 @@ static cudaError_t launch_td_bwd_t(const Tess &t, int nsteps, const AdjointPlan 
     st.h = (float)(1.0 / nsteps);
     st.hh = (float)(0.5 / nsteps);
     st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
-    const long long grid = (long long)nb * plan.parts;
-    if (grid == 0) return cudaSuccess;
-    kern<<<(unsigned)grid, plan.block, plan.smem, s>>>(t, nsteps, st, g, lin, table, grid_saved, C,
+    if (nb == 0) return cudaSuccess;
+    if (nb > 65535) return cudaErrorInvalidConfiguration;   // images on grid y
+    const dim3 grid((unsigned)plan.parts, (unsigned)nb);
+    kern<<<grid, plan.block, plan.smem, s>>>(t, nsteps, st, g, lin, table, grid_saved, C,
                                                        data, gout, ddata, partials, plan.parts,
                                                        plan.tiles, ties, err);
     return cudaGetLastError();

@@ -27,8 +27,8 @@ __global__ void __launch_bounds__(256)
     extern __shared__ float4 smem4[];
     __shared__ uint64_t bar;
     float *tab = reinterpret_cast<float *>(smem4);
-    const int th = blockIdx.x / tiles;
-    const int tile = blockIdx.x % tiles;
+    const int th = blockIdx.y;
+    const int tile = blockIdx.x;
     const int tab_floats = t.nC * P;
     if (!stage_table(tab, table + (long long)th * tab_floats, tab_floats, &bar, err)) return;
 
@@ -75,9 +75,9 @@ static cudaError_t launch_integrate_t(const Tess &t, int nsteps, const float *po
     constexpr int block = 256;
     const long long per = (long long)block * PPT;
     const int tiles = (int)((nP + per - 1) / per);
-    const long long grid = (long long)tiles * n_theta;
-    if (grid == 0) return cudaSuccess;
-    if (grid > 0x7fffffffll) return cudaErrorInvalidConfiguration;
+    if ((long long)tiles * n_theta == 0) return cudaSuccess;
+    if (n_theta > 65535) return cudaErrorInvalidConfiguration;   // theta on grid y
+    const dim3 grid((unsigned)tiles, (unsigned)n_theta);
     const size_t smem = (size_t)t.nC * N * (N + 1) * sizeof(float);
     auto kern = k_integrate<N, COMP, PPT>;
     if (smem > 48 * 1024) {
@@ -85,7 +85,7 @@ static cudaError_t launch_integrate_t(const Tess &t, int nsteps, const float *po
                                              (int)smem);
         if (e != cudaSuccess) return e;
     }
-    kern<<<(unsigned)grid, block, smem, s>>>(t, nsteps, points, broadcast, nP, table, tiles, out,
+    kern<<<grid, block, smem, s>>>(t, nsteps, points, broadcast, nP, table, tiles, out,
                                              trace, ties, err);
     return cudaGetLastError();
 }

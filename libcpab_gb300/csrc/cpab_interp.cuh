@@ -6,39 +6,45 @@
 
 namespace cpab {
 
+// Per-image extents.  Per-image element counts are below 2^31 (checked by the
+// C ABI), so in-image indices are 32-bit: 64-bit integer division and
+// float->int64 conversion run on GB300's narrow FP64 pipe.
 struct Geo {
-    int size[3];      // data extent per axis (W, H, D)
-    int outsize[3];   // output extent per axis
-    long long nP;     // prod(outsize)
-    long long nD;     // prod(size)
+    int size[3];       // data extent per axis (W, H, D)
+    int outsize[3];    // output extent per axis
+    float sizem1[3];   // size - 1, as float (coordinate scale)
+    int nP;            // prod(outsize)
+    int nD;            // prod(size)
+    FastDiv dout[3];   // division by outsize[j]
 };
 
 template <int N>
 struct Corner {
-    long long off[1 << N];   // element offsets of the 2^N corners, corner bit j = axis j high
-    float f[N];              // lerp weights xd, yd, zd
+    int off[1 << N];   // element offsets of the 2^N corners, corner bit j = axis j high
+    float f[N];        // lerp weights xd, yd, zd
 };
 
+// x = p*(size-1); x0 = clamp(floor(x)), x1 = clamp(floor(x)+1); xd = x - x0.
+// Floor and clamp are done in float (NaN -> 0, huge -> edge, as a saturating
+// conversion does) and the small integers are read from the float bits.
 template <int N>
 __device__ __forceinline__ Corner<N> corners(const float (&p)[N], const Geo &g) {
     Corner<N> cr;
-    long long i0[N], i1[N];
+    int i0[N], i1[N];
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-        const float x = p[j] * (float)(g.size[j] - 1);
-        const float fl = floorf(x);
-        // floor() then int64 conversion as torch does; clamp into the data.
-        long long a = (fl != fl) ? 0ll : (long long)fl;
-        long long b = a + 1;
-        a = a < 0 ? 0 : (a > g.size[j] - 1 ? g.size[j] - 1 : a);
-        b = b < 0 ? 0 : (b > g.size[j] - 1 ? g.size[j] - 1 : b);
-        i0[j] = a;
-        i1[j] = b;
-        cr.f[j] = x - (float)a;
+        const float x = p[j] * g.sizem1[j];
+        const float k = round_small(x);
+        const float fl = (k > x) ? k - 1.f : k;
+        const float a = fminf(fmaxf(fl, 0.f), g.sizem1[j]);
+        const float b = fminf(fmaxf(fl + 1.f, 0.f), g.sizem1[j]);
+        i0[j] = small_float_to_int(a);
+        i1[j] = small_float_to_int(b);
+        cr.f[j] = x - a;
     }
 #pragma unroll
     for (int m = 0; m < (1 << N); ++m) {
-        long long o = 0;
+        int o = 0;
 #pragma unroll
         for (int j = 0; j < N; ++j) o = o * g.size[j] + (((m >> j) & 1) ? i1[j] : i0[j]);
         cr.off[m] = o;
@@ -72,16 +78,18 @@ __device__ __forceinline__ float lerp_corners(const float *D, const Corner<N> &c
 // Output element offset of point k within one (b, c) plane: [W_out(, H_out(, D_out))]
 // with the last axis fastest, while k has axis 0 fastest.
 template <int N>
-__device__ __forceinline__ long long out_offset(long long k, const Geo &g) {
+__device__ __forceinline__ int out_offset(int k, const Geo &g) {
     if constexpr (N == 1) return k;
     else if constexpr (N == 2) {
-        const long long ix = k % g.outsize[0], iy = k / g.outsize[0];
-        return ix * g.outsize[1] + iy;
+        const unsigned iy = fast_div((unsigned)k, g.dout[0]);
+        const unsigned ix = (unsigned)k - iy * g.outsize[0];
+        return (int)(ix * g.outsize[1] + iy);
     } else {
-        const long long ix = k % g.outsize[0];
-        const long long r = k / g.outsize[0];
-        const long long iy = r % g.outsize[1], iz = r / g.outsize[1];
-        return (ix * g.outsize[1] + iy) * g.outsize[2] + iz;
+        const unsigned r = fast_div((unsigned)k, g.dout[0]);
+        const unsigned ix = (unsigned)k - r * g.outsize[0];
+        const unsigned iz = fast_div(r, g.dout[1]);
+        const unsigned iy = r - iz * g.outsize[1];
+        return (int)((ix * g.outsize[1] + iy) * g.outsize[2] + iz);
     }
 }
 
@@ -124,12 +132,26 @@ inline Geo make_geo(int ndim, const int *size, const int *outsize) {
     for (int j = 0; j < 3; ++j) {
         g.size[j] = j < ndim ? size[j] : 1;
         g.outsize[j] = j < ndim ? outsize[j] : 1;
+        g.sizem1[j] = (float)(g.size[j] - 1);
+        g.dout[j] = make_fastdiv((unsigned)g.outsize[j]);
     }
     for (int j = 0; j < ndim; ++j) {
         g.nP *= outsize[j];
         g.nD *= size[j];
     }
     return g;
+}
+
+// Per-image element counts must stay below 2^31 and extents below 2^22
+// (exact float coordinates); checked by the C ABI before make_geo.
+inline bool geo_fits(int ndim, const int *size, const int *outsize) {
+    long long nP = 1, nD = 1;
+    for (int j = 0; j < ndim; ++j) {
+        if (size[j] >= (1 << 22) || outsize[j] >= (1 << 22)) return false;
+        nP *= outsize[j];
+        nD *= size[j];
+    }
+    return nP < (1ll << 31) && nD < (1ll << 31);
 }
 
 }  // namespace cpab
