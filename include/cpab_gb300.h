@@ -127,6 +127,30 @@ CPAB_API int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const 
                   unsigned long long *ties, void *stream);
 
 /*
+ * cpab_backward for callers that cannot allocate device memory (a host
+ * runtime that owns all device memory through its own pool, or code running
+ * where allocation is not allowed) and so cannot supply a workspace.  No
+ * counterpart in the reference.
+ *
+ * Same arguments and results as cpab_backward minus the workspace.  Its
+ * scratch is a fixed 8 MiB array (2,097,152 floats) in the library's device
+ * memory, reserved on every GPU that loads the library until the process
+ * exits; problems with n_theta * nC * ndim * (ndim+1) above 2,097,152 are
+ * rejected with CPAB_ERR_WORKSPACE.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) with that device current: make it
+ * before capturing a stream.  All calls share the array (each call writes
+ * what it reads, no clearing needed); calls that may overlap on the GPU race
+ * and must be serialised by the caller.  It calls no cudaMalloc, cudaFree or
+ * allocating library routine.
+ */
+CPAB_API int cpab_backward_noalloc(int ndim, const int *nc, int nsteps, int mode,
+                                   const float *points, int broadcast, long long nP,
+                                   const float *A, const float *E, int n_theta,
+                                   const float *basis, int d, const float *grad_out,
+                                   float *dtheta, float *dpoints, unsigned long long *ties,
+                                   void *stream);
+
+/*
  * Linear / bilinear / trilinear sampling with clamp-to-edge.  grid is
  * [nb, ndim, prod(outsize)] with the meshgrid's x fastest; out is the image
  * layout above.  Replaces libcpab/pytorch/interpolation.py:12-172.

@@ -35,6 +35,8 @@ _SIGS = {
     'cpab_backward_workspace': ([_i, _c_int_p, _i, _ll, _i], _sz),
     'cpab_backward': ([_i, _c_int_p, _i, _i, _vp, _i, _ll, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp,
                        _vp, _sz, _vp, _vp], _i),
+    'cpab_backward_noalloc': ([_i, _c_int_p, _i, _i, _vp, _i, _ll, _vp, _vp, _i, _vp, _i, _vp,
+                               _vp, _vp, _vp, _vp], _i),
     'cpab_interpolate': ([_i, _vp, _i, _i, _c_int_p, _vp, _c_int_p, _vp, _vp], _i),
     'cpab_interpolate_backward': ([_i, _vp, _i, _i, _c_int_p, _vp, _c_int_p, _vp, _vp, _vp, _vp],
                                   _i),

@@ -373,3 +373,114 @@ int cpab_device_status(unsigned *flags, int clear) {
 }
 
 }  // extern "C"
+
+// --------------------------------------------------------------------------
+// cpab_backward without a caller-provided workspace.
+//
+// Some callers cannot allocate device memory at the point where they need a
+// gradient: a host runtime that owns all device memory through its own pool
+// and hands out only the tensors of the computation, or code running where
+// allocation is not permitted.  They cannot call cudaMalloc (or have torch do
+// it) to obtain the scratch that cpab_backward needs.  This variant keeps
+// that scratch -- the per-CTA partial cell gradients -- in a fixed array in
+// the library's device memory instead.
+//
+// * The array holds kNoAllocScratchFloats floats (8 MiB).  Every GPU that
+//   loads this library reserves it until the process exits.
+// * A problem needs n_theta * nC * ndim * (ndim + 1) floats per CTA slice;
+//   the variant uses as many CTAs per theta as fit (at most as many as
+//   cpab_backward would) and rejects problems where a single slice per theta
+//   does not fit.
+// * The array's device address is looked up with cudaGetSymbolAddress on the
+//   first call on each device (with that device current).  Make that first
+//   call before capturing the stream into a CUDA graph.
+// * The adjoint kernel writes every scratch element it later reads, so no
+//   clearing is needed, and the array keeps the last call's values.  All
+//   calls share the one array: calls that can overlap on the GPU (different
+//   streams, or other host threads) race and must be serialised by the
+//   caller.
+// * Nothing here calls cudaMalloc, cudaFree or an allocating library routine.
+// --------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocScratchFloats = size_t(1) << 21;
+__device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];
+float *g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+float *noalloc_scratch(int *rc) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        *rc = cuda_fail(e, "cudaGetDevice");
+        return nullptr;
+    }
+    if (dev < 0 || dev >= kMaxDevices) {
+        *rc = fail(CPAB_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+        return nullptr;
+    }
+    if (!g_noalloc_ptr[dev]) {
+        float *ptr = nullptr;
+        e = cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr) {
+            *rc = cuda_fail(e, "cudaGetSymbolAddress of the no-alloc scratch");
+            return nullptr;
+        }
+        g_noalloc_ptr[dev] = ptr;
+    }
+    *rc = CPAB_OK;
+    return g_noalloc_ptr[dev];
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpab_backward_noalloc(int ndim, const int *nc, int nsteps, int mode, const float *points,
+                          int broadcast, long long nP, const float *A, const float *E,
+                          int n_theta, const float *basis, int d, const float *grad_out,
+                          float *dtheta, float *dpoints, unsigned long long *ties,
+                          void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+        return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
+    if (nP < 0 || n_theta < 0 || d < 0) return fail(CPAB_ERR_ARGUMENT, "invalid sizes");
+    if ((rc = check_theta_count(n_theta))) return rc;
+    if (n_theta == 0 || (d == 0 && !dpoints)) return CPAB_OK;
+    if (!A || (d > 0 && (!dtheta || !basis)))
+        return fail(CPAB_ERR_ARGUMENT, "dtheta, basis or A is NULL");
+    if (mode == CPAB_GRAD_EXACT && !E) return fail(CPAB_ERR_ARGUMENT, "exact mode needs E");
+    cudaStream_t s = as_stream(stream);
+    if (nP == 0) {
+        cudaError_t e = cudaMemsetAsync(dtheta, 0, (size_t)n_theta * d * sizeof(float), s);
+        return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "memset");
+    }
+    if (!points || !grad_out) return fail(CPAB_ERR_ARGUMENT, "points or grad_out is NULL");
+    const size_t slice = (size_t)n_theta * t.nC * ndim * (ndim + 1);
+    if (slice > kNoAllocScratchFloats)
+        return fail(CPAB_ERR_WORKSPACE,
+                    "no-alloc scratch holds %zu floats; this problem needs at least %zu "
+                    "(n_theta * nC * ndim * (ndim+1)); use cpab_backward with a workspace",
+                    kNoAllocScratchFloats, slice);
+    AdjointPlan plan;
+    if (!plan_adjoint(t, nsteps, nP, n_theta, &plan))
+        return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
+    const long long fit = (long long)(kNoAllocScratchFloats / slice);
+    if (plan.parts > fit) plan.parts = (int)fit;
+    plan.partial_floats = slice * plan.parts;
+    float *partials = noalloc_scratch(&rc);
+    if (!partials) return rc;
+    unsigned *err = device_error_word();
+    cudaError_t e = launch_adjoint(t, nsteps, mode, plan, points, broadcast ? 1 : 0, nP,
+                                   mode == CPAB_GRAD_EXACT ? E : A, n_theta, grad_out, dpoints,
+                                   partials, ties, err, s);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+    if (d == 0) return CPAB_OK;
+    e = launch_finalize(t, nsteps, mode, partials, plan.parts, A, basis, d, n_theta, dtheta, s);
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "finalize launch");
+}
+
+}  // extern "C"
