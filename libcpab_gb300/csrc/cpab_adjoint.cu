@@ -18,25 +18,30 @@
 //     so with lambda_N = dL/dp_N and lambda_n = M^T lambda_{n+1}:
 //     dL/dtheta_k = sum_n < B_k,c_n , G_n >,
 //     G_n = h lambda_{n+1} [pMid_n;1]^T + h^2/2 (A^T lambda_{n+1}) [p_n;1]^T.
-//     The result is the reference's analytic gradient up to rounding.
+//     G_n is linear in S_n = lambda_{n+1} [p_n;1]^T with cell-constant
+//     coefficients ([pMid;1] = (I + h/2 [A;0]) [p;1]), so the reverse pass only
+//     sums S per cell and propagates lambda with the per-cell D = M - I;
+//     k_finalize applies G = h S (I + h/2 [A;0])^T + h^2/2 A_lin^T S once per
+//     cell.  The result is the reference's analytic gradient up to rounding.
 //   mode 1 ("exact"): exact discrete adjoint of the forward map
 //     p' = p + E_c [p;1]:  dL/dT_c += lambda_{n+1} [p_n;1]^T,
 //     lambda_n = lambda_{n+1} + E_lin^T lambda_{n+1}; dL/dA then follows from
 //     the adjoint Frechet derivative of expm (k_finalize).
 //
 // No per-step state goes to global memory: the forward pass logs each step's
-// cell (1 or 2 bytes) and a checkpoint every S steps in shared memory; the
+// cell (1 or 2 bytes) and a checkpoint every kSeg steps in shared memory; the
 // reverse pass rebuilds each segment's positions from its checkpoint with the
-// logged cells (no cell lookups) into registers.
+// logged cells (no cell lookups) into a shared-memory segment buffer.
 //
-// Deterministic reduction: a thread accumulates its contribution for the
-// current cell in registers and flushes it when the cell changes.  Flushing
-// lanes of a warp are grouped by cell (match.any); each group is reduced with
-// shuffles in a fixed order and its leader adds the sum into the warp's own
-// copy of the cell-gradient table in shared memory.  At the end the warp
-// copies are summed in warp order into one partial per CTA, and k_finalize
-// sums the partials in CTA order.  No floating-point atomics are used, so the
-// result is bit-reproducible for a given GPU and input.
+// Deterministic reduction: a thread accumulates S for its current cell in
+// registers.  When it leaves the cell, it appends (cell, S) to its warp's
+// queue in shared memory, at the slot given by its rank among the lanes
+// leaving a cell at this step; when the queue is nearly full, one lane per
+// component adds the entries, in queue order, into the warp's own copy of
+// the cell-gradient table.  At the end the warp copies are summed in warp
+// order into one partial per CTA, and k_finalize sums the partials in CTA
+// order.  No floating-point atomics are used, so the result is
+// bit-reproducible for a given GPU and input.
 #include "cpab_adjoint.cuh"
 
 namespace cpab {
@@ -47,23 +52,15 @@ __global__ void __launch_bounds__(256)
               long long nP, const float *__restrict__ table, int parts, int tiles,
               const float *__restrict__ gout, float *__restrict__ dpoints,
               float *__restrict__ partials, unsigned long long *ties, unsigned *err) {
-    constexpr int P = N * (N + 1);
     extern __shared__ float4 smem4[];
     __shared__ uint64_t bar;
-    const int B = blockDim.x, tid = threadIdx.x, W = B / 32;
-    const int G = t.nC * P, Gr = round4(G);
-    const int nseg = (nsteps + kSeg - 1) / kSeg;
-    float *tab = reinterpret_cast<float *>(smem4);
-    float *gw = tab + Gr;
-    float *ck = gw + (size_t)W * Gr;
-    float *pb = ck + (size_t)nseg * N * B;
-    CT *cl = reinterpret_cast<CT *>(pb + (size_t)kSeg * N * B);
+    const int B = blockDim.x, tid = threadIdx.x;
+    const int G = t.nC * N * (N + 1);
+    const AdjSmem<N, CT> sm = carve_adjoint<N, CT>(reinterpret_cast<float *>(smem4), t.nC, nsteps);
 
     const int th = blockIdx.y, part = blockIdx.x;
-    if (!stage_table(tab, table + (long long)th * G, G, &bar, err)) return;
-    for (int i = tid; i < W * Gr; i += B) gw[i] = 0.f;
-    __syncthreads();
-    float *warp_tab = gw + (size_t)(tid >> 5) * Gr;
+    if (!adjoint_prologue<N, MODE, CT>(sm, table + (long long)th * G, t.nC, st, &bar, err)) return;
+    auto q = warp_queue<N, CT>(sm, t.nC);
     const float *src = points + (broadcast ? (long long)th * N * nP : 0ll);
 
     for (int tile = part; tile < tiles; tile += parts) {
@@ -72,22 +69,16 @@ __global__ void __launch_bounds__(256)
         float p[N], lam[N];
 #pragma unroll
         for (int r = 0; r < N; ++r) p[r] = live ? __ldg(src + r * nP + idx) : 0.5f;
-        logged_forward<N, MODE, CT>(tab, t, nsteps, st, p, ck, cl, ties, err);
+        logged_forward<N, MODE, CT>(sm, t, nsteps, st, p, ties, err);
 #pragma unroll
         for (int r = 0; r < N; ++r) lam[r] = live ? __ldg(gout + ((long long)th * N + r) * nP + idx) : 0.f;
-        reverse_sweep<N, MODE, CT>(tab, ck, cl, pb, nsteps, st, live, lam, warp_tab);
+        reverse_sweep<N, MODE, CT>(sm, nsteps, st, live, lam, q);
         if (dpoints && live) {
 #pragma unroll
             for (int r = 0; r < N; ++r) dpoints[((long long)th * N + r) * nP + idx] = lam[r];
         }
     }
-    __syncthreads();
-    float *dst = partials + ((long long)th * parts + part) * G;
-    for (int i = tid; i < G; i += B) {
-        float s = 0.f;
-        for (int w = 0; w < W; ++w) s += gw[(size_t)w * Gr + i];
-        dst[i] = s;
-    }
+    adjoint_epilogue<N, CT>(sm, q, t.nC, partials + ((long long)th * parts + part) * G);
 }
 
 // ------------------------------ planning -------------------------------------
@@ -275,7 +266,7 @@ __device__ __forceinline__ void frechet_expm(const float (&Y0)[K][K], const floa
 
 template <int N, int MODE>
 __global__ void __launch_bounds__(256)
-    k_finalize(int nC, float dt, const float *__restrict__ partials, int parts,
+    k_finalize(int nC, Steps st, const float *__restrict__ partials, int parts,
                const float *__restrict__ A, const float *__restrict__ basis, int d,
                float *__restrict__ dtheta) {
     constexpr int P = N * (N + 1);
@@ -290,7 +281,37 @@ __global__ void __launch_bounds__(256)
         g[i] = s;
     }
     __syncthreads();
-    if constexpr (MODE == 1) {
+    if constexpr (MODE == 0) {
+        // S_c = sum_n lambda_{n+1} [p_n;1]^T  ->
+        // G_c = h S_c (I + h/2 [A_c;0])^T + h^2/2 A_lin^T S_c
+        for (int c = tid; c < nC; c += B) {
+            const float *a = A + ((long long)th * nC + c) * P;
+            float S[N][N + 1], Gc[N][N + 1];
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+#pragma unroll
+                for (int j = 0; j <= N; ++j) S[i][j] = g[c * P + i * (N + 1) + j];
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+#pragma unroll
+                for (int j = 0; j <= N; ++j) {
+                    float x = 0.f, y = 0.f;
+                    if (j < N) {
+#pragma unroll
+                        for (int k = 0; k <= N; ++k) x = fmaf(S[i][k], a[j * (N + 1) + k], x);
+                    }
+#pragma unroll
+                    for (int r = 0; r < N; ++r) y = fmaf(a[r * (N + 1) + i], S[r][j], y);
+                    Gc[i][j] = fmaf(st.h, fmaf(st.hh, x, S[i][j]), st.hh2 * y);
+                }
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+#pragma unroll
+                for (int j = 0; j <= N; ++j) g[c * P + i * (N + 1) + j] = Gc[i][j];
+        }
+        __syncthreads();
+    } else {
+        const float dt = st.h;
         // dL/dT_c (top N rows) -> dL/dA_c = dt * [L_exp(X^T, [dL/dT_c; 0])]_{top rows}
         for (int c = tid; c < nC; c += B) {
             const float *a = A + ((long long)th * nC + c) * P;
@@ -323,7 +344,10 @@ cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *pa
     if (n_theta == 0) return cudaSuccess;
     const int P = t.ndim * (t.ndim + 1);
     const size_t smem = (size_t)t.nC * P * sizeof(float);
-    const float dt = (float)(1.0 / nsteps);
+    Steps st;
+    st.h = (float)(1.0 / nsteps);
+    st.hh = (float)(0.5 / nsteps);
+    st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
     const int block = 256;
 #define CPAB_FIN(N, M)                                                                         \
     {                                                                                          \
@@ -333,7 +357,7 @@ cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *pa
                 kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                 \
             if (e != cudaSuccess) return e;                                                    \
         }                                                                                      \
-        kern<<<n_theta, block, smem, s>>>(t.nC, dt, partials, parts, A, basis, d, dtheta);     \
+        kern<<<n_theta, block, smem, s>>>(t.nC, st, partials, parts, A, basis, d, dtheta);     \
         return cudaGetLastError();                                                             \
     }
     if (mode == 0) {

@@ -136,23 +136,15 @@ __global__ void __launch_bounds__(256)
                               const float *__restrict__ data, const float *__restrict__ gout,
                               float *__restrict__ ddata, float *__restrict__ partials, int parts,
                               int tiles, unsigned long long *ties, unsigned *err) {
-    constexpr int P = N * (N + 1);
     extern __shared__ float4 smem4[];
     __shared__ uint64_t bar;
-    const int B = blockDim.x, tid = threadIdx.x, W = B / 32;
-    const int G = t.nC * P, Gr = round4(G);
-    const int nseg = (nsteps + kSeg - 1) / kSeg;
-    float *tab = reinterpret_cast<float *>(smem4);
-    float *gw = tab + Gr;
-    float *ck = gw + (size_t)W * Gr;
-    float *pb = ck + (size_t)nseg * N * B;
-    CT *cl = reinterpret_cast<CT *>(pb + (size_t)kSeg * N * B);
+    const int B = blockDim.x, tid = threadIdx.x;
+    const int G = t.nC * N * (N + 1);
+    const AdjSmem<N, CT> sm = carve_adjoint<N, CT>(reinterpret_cast<float *>(smem4), t.nC, nsteps);
 
     const int b = blockIdx.y, part = blockIdx.x;
-    if (!stage_table(tab, table + (long long)b * G, G, &bar, err)) return;
-    for (int i = tid; i < W * Gr; i += B) gw[i] = 0.f;
-    __syncthreads();
-    float *warp_tab = gw + (size_t)(tid >> 5) * Gr;
+    if (!adjoint_prologue<N, MODE, CT>(sm, table + (long long)b * G, t.nC, st, &bar, err)) return;
+    auto q = warp_queue<N, CT>(sm, t.nC);
 
     for (int tile = part; tile < tiles; tile += parts) {
         const int o = tile * B + tid;
@@ -163,7 +155,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
             for (int r = 0; r < N; ++r) p[r] = 0.5f;
         }
-        logged_forward<N, MODE, CT>(tab, t, nsteps, st, p, ck, cl, ties, err);
+        logged_forward<N, MODE, CT>(sm, t, nsteps, st, p, ties, err);
 #pragma unroll
         for (int r = 0; r < N; ++r) {
             if constexpr (MODE == 1) pN[r] = p[r];
@@ -183,15 +175,9 @@ __global__ void __launch_bounds__(256)
         }
 #pragma unroll
         for (int r = 0; r < N; ++r) lam[r] = gf[r] * (float)(g.size[r] - 1);
-        reverse_sweep<N, MODE, CT>(tab, ck, cl, pb, nsteps, st, live, lam, warp_tab);
+        reverse_sweep<N, MODE, CT>(sm, nsteps, st, live, lam, q);
     }
-    __syncthreads();
-    float *dst = partials + ((long long)b * parts + part) * G;
-    for (int i = tid; i < G; i += B) {
-        float s = 0.f;
-        for (int w = 0; w < W; ++w) s += gw[(size_t)w * Gr + i];
-        dst[i] = s;
-    }
+    adjoint_epilogue<N, CT>(sm, q, t.nC, partials + ((long long)b * parts + part) * G);
 }
 
 template <int N, int MODE, typename CT>
