@@ -51,6 +51,8 @@ def parse():
                     help='images per step (the headline workload uses 64; smaller values '
                          'are for profiling runs only)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--no-ragged', action='store_true',
+                    help='skip the ragged 1D series leg (reported beside the headline)')
     args = ap.parse_args()
     return args
 
@@ -236,6 +238,22 @@ def run_gb300(args):
     t_bwd = time_events(lambda: N.transform_data_backward(NC, NSTEPS, 0, lin, [SIZE, SIZE], A, E,
                                                           grid, data, basis, gout,
                                                           workspace=ws), args.steps, flush)
+    # the plain one-kernel-per-op GPU path through the same public API:
+    # uniform_meshgrid -> transform_grid -> interpolate (libcpab/cpab.py:304-331
+    # unfused), with the same loss and gradients
+    mesh = T.uniform_meshgrid([SIZE, SIZE])
+
+    def step_unfused():
+        th = theta.detach().requires_grad_(True)
+        dd = data.detach().requires_grad_(True)
+        out = T.interpolate(dd, T.transform_grid(mesh, th), [SIZE, SIZE])
+        loss = F.mse_loss(out, target)
+        loss.backward()
+        return loss
+    for _ in range(2):
+        step_unfused()
+    t_unf = time_events(step_unfused, args.steps, flush)
+    ragged = run_ragged(device, args.steps, flush) if rank == 0 and not args.no_ragged else None
     clk = clocks.stop() if clocks else None
     status = N.device_status()
 
@@ -280,11 +298,93 @@ def run_gb300(args):
                                'flop_per_launch': pts * NSTEPS * FLOP_FWD_STEP,
                                'tflops': pts * NSTEPS * FLOP_FWD_STEP / (fwd_ms / 1e3) / 1e12,
                                'interp_gbs': fwd_bytes / (fwd_ms / 1e3) / 1e9},
+            'unfused_gpu': {'path': 'transform_grid -> interpolate -> MSE, autograd '
+                                    '(cpab_integrate, cpab_interpolate and their backward '
+                                    'kernels, one launch per op)',
+                            'ms_per_step': sum(t_unf) / len(t_unf),
+                            'value': pts / (sum(t_unf) / len(t_unf) / 1e3),
+                            'unit': 'points/s'},
+            'ragged_1d': ragged,
             'clocks': clk, 'device_status': status,
         }
     if world > 1:
         torch.distributed.destroy_process_group()
     return result
+
+
+# ragged batched 1D series: 4,096 series, lengths U{32..4096}, tess [100]
+RAGGED_S, RAGGED_NC, RAGGED_LEN = 4096, 100, (32, 4096)
+
+
+def ragged_inputs(T, device):
+    """Series values = sum of 3 sinusoids (f ~ U[1,10], phase ~ U[0,2pi],
+    amplitude ~ U[0.5,1.5]) + N(0, 0.1^2) on linspace(0, 1, L_s); theta ~ N(0, I)
+    (seed 0), data (seed 1), target = the values warped by a second theta
+    (seed 2)."""
+    from libcpab_gb300 import _native as N
+    from libcpab_gb300.functions import basis_on
+    d = T.get_theta_dim()
+    g0, g1, g2 = (torch.Generator().manual_seed(k) for k in (0, 1, 2))
+    theta = torch.randn(RAGGED_S, d, generator=g0)
+    lengths = torch.randint(RAGGED_LEN[0], RAGGED_LEN[1] + 1, (RAGGED_S,), generator=g1)
+    off = torch.cat([torch.zeros(1, dtype=torch.int64), torch.cumsum(lengths, 0)])
+    sid = torch.repeat_interleave(torch.arange(RAGGED_S), lengths)
+    j = torch.arange(int(off[-1])) - off[sid]
+    x = j.double() / (lengths[sid] - 1).double()
+    f = 1 + 9 * torch.rand(RAGGED_S, 3, generator=g1, dtype=torch.float64)
+    ph = 2 * np.pi * torch.rand(RAGGED_S, 3, generator=g1, dtype=torch.float64)
+    amp = 0.5 + torch.rand(RAGGED_S, 3, generator=g1, dtype=torch.float64)
+    v = (amp[sid] * torch.sin(2 * np.pi * f[sid] * x[:, None] + ph[sid])).sum(1)
+    v = v + 0.1 * torch.randn(v.shape, generator=g1, dtype=torch.float64)
+    values = v.float().to(device)
+    off = off.to(device)
+    theta2 = torch.randn(RAGGED_S, d, generator=g2).to(device)
+    basis = basis_on(T.params, device)
+    _, _, E2 = N.cell_tables([RAGGED_NC], NSTEPS, theta2, basis)
+    target = N.ragged_forward([RAGGED_NC], NSTEPS, E2, off, values)
+    return theta.to(device), off, values, target, basis
+
+
+def run_ragged(device, steps, flush):
+    """Fused forward + MSE + dtheta/d(values) adjoint of the ragged workload in
+    one persistent launch (plus the tile-prefix and finalize kernels and the
+    cell tables), autotuned, captured in a CUDA graph and replayed."""
+    from libcpab_gb300 import Cpab, _native as N
+    T = Cpab([RAGGED_NC], backend='pytorch', device='gpu', zero_boundary=False)
+    theta, off, values, target, basis = ragged_inputs(T, device)
+    total = values.numel()
+    A, _, E = N.cell_tables([RAGGED_NC], NSTEPS, theta, basis)
+    ws = N.ragged_workspace(RAGGED_NC, NSTEPS, RAGGED_S, device)
+    shape_f, ms_f, _ = N.ragged_tune(0, [RAGGED_NC], NSTEPS, 0, A, E, off, values, target, basis,
+                                     workspace=ws)
+    shape_b, ms_b, _ = N.ragged_tune(1, [RAGGED_NC], NSTEPS, 0, A, E, off, values, target, basis,
+                                     workspace=ws)
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(st):
+        for _ in range(3):
+            A, _, E = N.cell_tables([RAGGED_NC], NSTEPS, theta, basis)
+            N.ragged_mse([RAGGED_NC], NSTEPS, 0, A, E, off, values, target, basis, workspace=ws)
+    torch.cuda.current_stream().wait_stream(st)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        A, _, E = N.cell_tables([RAGGED_NC], NSTEPS, theta, basis)
+        res = N.ragged_mse([RAGGED_NC], NSTEPS, 0, A, E, off, values, target, basis,
+                           workspace=ws)
+    for _ in range(3):
+        g.replay()
+    times = time_events(g.replay, steps, flush)
+    ms = sum(times) / len(times)
+    loss = float(res['sse'].sum()) / total
+    return {'workload': 'ragged 1D: %d series, lengths U{%d..%d} (total %d points), tess [%d] '
+                        'zero_boundary=False, theta ~ N(0,I), sum-of-sinusoids values, MSE vs '
+                        'values warped by a second theta, fwd + dtheta/d(values) (reference '
+                        'gradient) in one persistent launch, CUDA-graph replay'
+                        % (RAGGED_S, RAGGED_LEN[0], RAGGED_LEN[1], total, RAGGED_NC),
+            'value': total / (ms / 1e3), 'unit': 'points/s', 'ms_per_step': ms,
+            'launches_per_step': 4, 'tuned_shape_fused': list(shape_b),
+            'tuned_shape_forward': list(shape_f), 'forward_only_ms': ms_f,
+            'loss': loss}
 
 
 def cpu_reference_step(sample, orc, T_h, nc):

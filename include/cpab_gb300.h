@@ -51,6 +51,8 @@ extern "C" {
 /* Bits reported by cpab_device_status. */
 #define CPAB_DEV_TMA_TIMEOUT 1u /* a bulk copy to shared memory did not complete */
 #define CPAB_DEV_BAD_CELL 2u    /* a cell index fell outside [0, nC)             */
+#define CPAB_DEV_SCRATCH 4u     /* a kernel's scratch region was too small       */
+#define CPAB_DEV_BAD_OFFSETS 8u /* a ragged series had invalid offsets (skipped) */
 
 /* Message of the calling thread's last error ("" if none). */
 CPAB_API const char *cpab_last_error(void);
@@ -205,6 +207,79 @@ CPAB_API int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, i
  */
 CPAB_API int cpab_findcellidx(int ndim, const int *nc, const float *points, long long nP, int *out,
                      unsigned long long *ties, void *stream);
+
+/*
+ * Ragged batched 1D series.  No single reference entry point: the reference
+ * processes each series as its own Cpab.transform_data call (libcpab/cpab.py:
+ * 304-331) with outsize [L_s], i.e. grid = torch.linspace(0, 1, L_s)
+ * (libcpab/pytorch/functions.py:102-108), transform_grid with that series'
+ * theta (libcpab/pytorch/transformer.py:72-87, the cpab_gpu.forward /
+ * cpab_gpu.backward pair of libcpab/pytorch/transformer_cuda.cpp:17-70) and
+ * linear interpolation (libcpab/pytorch/interpolation.py:18-60).  These
+ * entry points run all S series in one persistent launch.
+ *
+ * Series s owns values[offsets[s] .. offsets[s+1]) (L_s = offsets[s+1] -
+ * offsets[s] points, 0 <= L_s < 2^22); offsets is a DEVICE array of S + 1
+ * int64 (a series with invalid offsets is skipped and raises
+ * CPAB_DEV_BAD_OFFSETS).  total = number of value elements; total + 128*S
+ * must be below 2^31.  A and E are [S, nC, 1, 2] (one theta per series, from
+ * cpab_cell_tables); basis is [2*nC, d]; dtheta is [S, d].  workspace is
+ * device memory of cpab_ragged1d_workspace() bytes (warp-tile prefix and the
+ * deterministic partial sums); the calls do not synchronise and can be
+ * captured in a CUDA graph.
+ */
+CPAB_API size_t cpab_ragged1d_workspace(int nc, int nsteps, int S);
+
+/* out[offsets[s] + j] = interp(values_s, T_s(linspace(0, 1, L_s)[j])). */
+CPAB_API int cpab_ragged1d_forward(int nc, int nsteps, const float *E, int S,
+                                   const long long *offsets, long long total,
+                                   const float *values, float *out, void *workspace,
+                                   size_t workspace_bytes, unsigned long long *ties,
+                                   void *stream);
+
+/*
+ * Backward of cpab_ragged1d_forward from grad_out = dL/d(out): dtheta [S, d]
+ * (overwritten) and dvalues [total] (overwritten, may be NULL; scatter-add
+ * with float atomics like the reference's autograd).  Mode as in
+ * cpab_backward.
+ */
+CPAB_API int cpab_ragged1d_backward(int nc, int nsteps, int mode, const float *A, const float *E,
+                                    int S, const long long *offsets, long long total,
+                                    const float *basis, int d, const float *values,
+                                    const float *grad_out, float *dtheta, float *dvalues,
+                                    void *workspace, size_t workspace_bytes,
+                                    unsigned long long *ties, void *stream);
+
+/*
+ * Forward, squared-error loss and backward in one launch (plus the prefix
+ * and finalize kernels): out (may be NULL) as cpab_ragged1d_forward, sse[s] =
+ * sum_j (out - target)^2 over series s, and the gradients of
+ * L = sum_s loss_scale/2 * sse[s] (loss_scale = 2/total gives the mean
+ * squared error): dtheta [S, d] and dvalues (may be NULL).
+ */
+CPAB_API int cpab_ragged1d_mse(int nc, int nsteps, int mode, const float *A, const float *E, int S,
+                               const long long *offsets, long long total, const float *basis,
+                               int d, const float *values, const float *target, float loss_scale,
+                               float *out, float *sse, float *dtheta, float *dvalues,
+                               void *workspace, size_t workspace_bytes,
+                               unsigned long long *ties, void *stream);
+
+/*
+ * Autotuner: times the launch shapes (threads per block 64/128/256 x points
+ * per lane 1/2/4) of the ragged forward (kind 0) or adjoint (kind 1, timed
+ * as cpab_ragged1d_mse) kernels on these inputs, keeps the fastest for later
+ * calls with the same (device, kind, mode, nc, nsteps, S, total), and leaves
+ * the outputs of the chosen shape in out (kind 0) or out/sse/dtheta/dvalues
+ * (kind 1).  shape (may be NULL) receives {threads, points per lane};
+ * best_ms (may be NULL) the fastest time.  Synchronises the stream; refuses
+ * to run while the stream is being captured.
+ */
+CPAB_API int cpab_ragged1d_tune(int kind, int nc, int nsteps, int mode, const float *A,
+                                const float *E, int S, const long long *offsets, long long total,
+                                const float *basis, int d, const float *values,
+                                const float *target, float loss_scale, float *out, float *sse,
+                                float *dtheta, float *dvalues, void *workspace,
+                                size_t workspace_bytes, int *shape, float *best_ms, void *stream);
 
 /*
  * Synchronise the current device and report the device error word (the

@@ -5,6 +5,8 @@ TransformGridNumeric -- forward differences in theta, the scheme the reference's
                   numeric_grad option intends (libcpab/pytorch/transformer.py:205-295)
 Interpolate    -- interpolation with its backward (libcpab/pytorch/interpolation.py)
 TransformData  -- fused meshgrid -> integrate -> sample (libcpab/cpab.py:304-331)
+TransformDataRagged -- the same for many 1D series of uneven lengths in one
+                  persistent launch (one theta per series)
 
 Gradient modes (params.gradient):
   'reference' -- the reference's analytic gradient: the midpoint-rule
@@ -153,3 +155,31 @@ class TransformData(torch.autograd.Function):
             _basis(params, data.device), grad.to(torch.float32).contiguous(), want_ddata=want_d,
             ties=_ties(params))
         return ddata, (dtheta if want_t else None), None, None
+
+
+class TransformDataRagged(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, values, theta, offsets, params):
+        values_c = values.detach().to(torch.float32).contiguous()
+        theta_c = theta.detach().to(torch.float32).contiguous()
+        basis = _basis(params, values.device)
+        A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis)
+        out = N.ragged_forward(params.nc, params.nstepsolver, E, offsets, values_c,
+                               ties=_ties(params))
+        ctx.save_for_backward(values_c, offsets, A, E)
+        ctx.params = params
+        return out
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, grad):
+        values, offsets, A, E = ctx.saved_tensors
+        params = ctx.params
+        want_v, want_t = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        if not (want_v or want_t):
+            return None, None, None, None
+        dtheta, dvalues = N.ragged_backward(
+            params.nc, params.nstepsolver, _mode(params), A, E, offsets, values,
+            _basis(params, values.device), grad.to(torch.float32).contiguous(),
+            want_dvalues=want_v, ties=_ties(params))
+        return dvalues, (dtheta if want_t else None), None, None

@@ -48,6 +48,15 @@ _SIGS = {
                                      _i),
     'cpab_findcellidx': ([_i, _c_int_p, _vp, _ll, _vp, _vp, _vp], _i),
     'cpab_device_status': ([ctypes.POINTER(ctypes.c_uint), _i], _i),
+    'cpab_ragged1d_workspace': ([_i, _i, _i], _sz),
+    'cpab_ragged1d_forward': ([_i, _i, _vp, _i, _vp, _ll, _vp, _vp, _vp, _sz, _vp, _vp], _i),
+    'cpab_ragged1d_backward': ([_i, _i, _i, _vp, _vp, _i, _vp, _ll, _vp, _i, _vp, _vp, _vp, _vp,
+                                _vp, _sz, _vp, _vp], _i),
+    'cpab_ragged1d_mse': ([_i, _i, _i, _vp, _vp, _i, _vp, _ll, _vp, _i, _vp, _vp, ctypes.c_float,
+                           _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp], _i),
+    'cpab_ragged1d_tune': ([_i, _i, _i, _i, _vp, _vp, _i, _vp, _ll, _vp, _i, _vp, _vp,
+                            ctypes.c_float, _vp, _vp, _vp, _vp, _vp, _sz, _c_int_p,
+                            ctypes.POINTER(ctypes.c_float), _vp], _i),
 }
 
 EXPORTED = tuple(_SIGS)
@@ -301,3 +310,99 @@ def device_status(clear=True) -> int:
     flags = ctypes.c_uint(0)
     _check(load().cpab_device_status(ctypes.byref(flags), int(bool(clear))))
     return flags.value
+
+
+# ------------------------- ragged batched 1D series ------------------------- #
+def _ragged_common(nc, offsets, values):
+    if len(nc) != 1:
+        raise ValueError('ragged series are 1D (nc has %d entries)' % len(nc))
+    _require(offsets, 'offsets', torch.int64)
+    _require(values, 'values')
+    if offsets.dim() != 1 or offsets.numel() < 1:
+        raise ValueError('offsets must be a 1D tensor of S + 1 entries')
+    return int(nc[0]), offsets.numel() - 1, values.numel()
+
+
+def ragged_workspace(nc, nsteps, S, device, workspace=None):
+    need = load().cpab_ragged1d_workspace(int(nc), int(nsteps), int(S))
+    if need == 0 and S > 0:
+        _check(1)
+    if workspace is None or workspace.numel() < need:
+        workspace = torch.empty(max(need, 1), device=device, dtype=torch.uint8)
+    return workspace
+
+
+def ragged_forward(nc, nsteps, E, offsets, values, ties=None, workspace=None):
+    """Warped values of every series, [total] (same offsets as values)."""
+    n, S, total = _ragged_common(nc, offsets, values)
+    _require(E, 'E')
+    dev = values.device
+    out = torch.empty_like(values)
+    ws = ragged_workspace(n, nsteps, S, dev, workspace)
+    _check(load().cpab_ragged1d_forward(n, int(nsteps), _ptr(E), S, _ptr(offsets), total,
+                                        _ptr(values), _ptr(out), _ptr(ws), ws.numel(), _ptr(ties),
+                                        _stream(dev)))
+    return out
+
+
+def ragged_backward(nc, nsteps, mode, A, E, offsets, values, basis, grad_out, want_dvalues=True,
+                    ties=None, workspace=None):
+    """(dtheta [S, d], dvalues [total] or None) from dL/d(out)."""
+    n, S, total = _ragged_common(nc, offsets, values)
+    for t, name in ((A, 'A'), (E, 'E'), (basis, 'basis'), (grad_out, 'grad_out')):
+        _require(t, name)
+    dev = values.device
+    d = basis.shape[1]
+    dtheta = torch.empty((S, d), device=dev, dtype=torch.float32)
+    dvalues = torch.empty_like(values) if want_dvalues else None
+    ws = ragged_workspace(n, nsteps, S, dev, workspace)
+    _check(load().cpab_ragged1d_backward(n, int(nsteps), int(mode), _ptr(A), _ptr(E), S,
+                                         _ptr(offsets), total, _ptr(basis), d, _ptr(values),
+                                         _ptr(grad_out), _ptr(dtheta), _ptr(dvalues), _ptr(ws),
+                                         ws.numel(), _ptr(ties), _stream(dev)))
+    return dtheta, dvalues
+
+
+def _mse_args(nc, nsteps, mode, A, E, offsets, values, target, basis, loss_scale, want_out,
+              want_dvalues, workspace):
+    n, S, total = _ragged_common(nc, offsets, values)
+    for t, name in ((A, 'A'), (E, 'E'), (basis, 'basis'), (target, 'target')):
+        _require(t, name)
+    dev = values.device
+    d = basis.shape[1]
+    if loss_scale is None:
+        loss_scale = 2.0 / max(total, 1)
+    res = {
+        'out': torch.empty_like(values) if want_out else None,
+        'sse': torch.empty((S,), device=dev, dtype=torch.float32),
+        'dtheta': torch.empty((S, d), device=dev, dtype=torch.float32),
+        'dvalues': torch.empty_like(values) if want_dvalues else None,
+    }
+    ws = ragged_workspace(n, nsteps, S, dev, workspace)
+    args = (n, int(nsteps), int(mode), _ptr(A), _ptr(E), S, _ptr(offsets), total, _ptr(basis), d,
+            _ptr(values), _ptr(target), float(loss_scale), _ptr(res['out']), _ptr(res['sse']),
+            _ptr(res['dtheta']), _ptr(res['dvalues']), _ptr(ws), ws.numel())
+    return args, res, dev
+
+
+def ragged_mse(nc, nsteps, mode, A, E, offsets, values, target, basis, loss_scale=None,
+               want_out=False, want_dvalues=True, ties=None, workspace=None):
+    """Fused forward + squared-error loss + backward.  Returns a dict with
+    out (or None), sse [S], dtheta [S, d] and dvalues (or None); the loss is
+    loss_scale/2 * sse.sum() (loss_scale defaults to 2/total: the MSE)."""
+    args, res, dev = _mse_args(nc, nsteps, mode, A, E, offsets, values, target, basis,
+                               loss_scale, want_out, want_dvalues, workspace)
+    _check(load().cpab_ragged1d_mse(*args, _ptr(ties), _stream(dev)))
+    return res
+
+
+def ragged_tune(kind, nc, nsteps, mode, A, E, offsets, values, target, basis, loss_scale=None,
+                workspace=None):
+    """Autotune the ragged forward (kind 0) or adjoint (kind 1) launch shape on
+    these inputs.  Returns ((threads, points per lane), best ms, outputs)."""
+    args, res, dev = _mse_args(nc, nsteps, mode, A, E, offsets, values, target, basis,
+                               loss_scale, True, True, workspace)
+    shape = (ctypes.c_int * 2)(0, 0)
+    ms = ctypes.c_float(0.0)
+    _check(load().cpab_ragged1d_tune(int(kind), *args, shape, ctypes.byref(ms), _stream(dev)))
+    return (shape[0], shape[1]), ms.value, res

@@ -198,6 +198,22 @@ class Cpab(object):
         self._check_type(theta); self._check_device(theta)
         return self.backend.transform_data(data, theta, self.params, outsize)
 
+    def transform_data_ragged(self, values, offsets, theta):
+        """Ragged batch of 1D series (extension; no reference counterpart):
+        series s = values[offsets[s]:offsets[s+1]] warped by theta[s] as
+        transform_data(values_s[None, None], theta[s:s+1], [L_s]) would, all
+        in one launch.  values [total] float32, offsets [S+1] int64 (CUDA)."""
+        self._check_type(values); self._check_device(values)
+        self._check_type(theta); self._check_device(theta)
+        return self.backend.transform_data_ragged(values, offsets, theta, self.params)
+
+    def ragged_mse(self, values, target, offsets, theta, **kwargs):
+        """Fused forward + mean-squared-error loss + backward for ragged 1D
+        series (extension).  Returns a dict with loss, sse, dtheta, dvalues."""
+        self._check_type(values); self._check_device(values)
+        self._check_type(theta); self._check_device(theta)
+        return self.backend.ragged_mse(values, target, offsets, theta, self.params, **kwargs)
+
     def calc_vectorfield(self, grid, theta):
         self._check_type(grid); self._check_device(grid)
         self._check_type(theta); self._check_device(theta)

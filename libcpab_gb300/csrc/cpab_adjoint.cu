@@ -34,14 +34,14 @@
 // logged cells (no cell lookups) into a shared-memory segment buffer.
 //
 // Deterministic reduction: a thread accumulates S for its current cell in
-// registers.  When it leaves the cell, it appends (cell, S) to its warp's
-// queue in shared memory, at the slot given by its rank among the lanes
-// leaving a cell at this step; when the queue is nearly full, one lane per
-// component adds the entries, in queue order, into the warp's own copy of
-// the cell-gradient table.  At the end the warp copies are summed in warp
-// order into one partial per CTA, and k_finalize sums the partials in CTA
-// order.  No floating-point atomics are used, so the result is
-// bit-reproducible for a given GPU and input.
+// registers.  At each step the lanes that leave a cell add their S into the
+// warp's own copy of the cell-gradient table in one pass; lanes leaving the
+// same cell at the same step are first summed in lane order (match.any and
+// shuffles), so each table element receives at most one add per step, in
+// step order.  At the end the warp copies are summed in warp order into one
+// partial per CTA, and k_finalize sums the partials in CTA order.  No
+// floating-point atomics are used, so the result is bit-reproducible for a
+// given GPU and input.
 #include "cpab_adjoint.cuh"
 
 namespace cpab {
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256)
 
     const int th = blockIdx.y, part = blockIdx.x;
     if (!adjoint_prologue<N, MODE, CT>(sm, table + (long long)th * G, t.nC, st, &bar, err)) return;
-    auto q = warp_queue<N, CT>(sm, t.nC);
+    float *warp_tab = sm.gw + (size_t)(tid >> 5) * round4(G);
     const float *src = points + (broadcast ? (long long)th * N * nP : 0ll);
 
     for (int tile = part; tile < tiles; tile += parts) {
@@ -72,13 +72,13 @@ __global__ void __launch_bounds__(256)
         logged_forward<N, MODE, CT>(sm, t, nsteps, st, p, ties, err);
 #pragma unroll
         for (int r = 0; r < N; ++r) lam[r] = live ? __ldg(gout + ((long long)th * N + r) * nP + idx) : 0.f;
-        reverse_sweep<N, MODE, CT>(sm, nsteps, st, live, lam, q);
+        reverse_sweep<N, MODE, CT>(sm, nsteps, st, live, lam, warp_tab);
         if (dpoints && live) {
 #pragma unroll
             for (int r = 0; r < N; ++r) dpoints[((long long)th * N + r) * nP + idx] = lam[r];
         }
     }
-    adjoint_epilogue<N, CT>(sm, q, t.nC, partials + ((long long)th * parts + part) * G);
+    adjoint_epilogue<N, CT>(sm, t.nC, partials + ((long long)th * parts + part) * G);
 }
 
 // ------------------------------ planning -------------------------------------
@@ -189,81 +189,6 @@ cudaError_t launch_adjoint(const Tess &t, int nsteps, int mode, const AdjointPla
 }
 
 // ------------------------------ finalize -------------------------------------
-// Frechet derivative of expm at Y in direction E, by a truncated Horner
-// recursion on Y/2^s, E/2^s followed by s squarings:
-//   R_{k-1} = I + (Y/k) R_k,  dR_{k-1} = (E/k) R_k + (Y/k) dR_k,
-//   then  L <- L R + R L,  R <- R R.
-template <int K>
-__device__ __forceinline__ void frechet_expm(const float (&Y0)[K][K], const float (&E0)[K][K],
-                                             float (&L)[K][K]) {
-    float norm = 0.f;
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-        float s = 0.f;
-#pragma unroll
-        for (int i = 0; i < K; ++i) s += fabsf(Y0[i][j]);
-        norm = fmaxf(norm, s);
-    }
-    int sq = 0;
-    if (norm > 0.5f) sq = min(64, (int)ceilf(log2f(norm / 0.5f)));
-    const float sc = ldexpf(1.f, -sq);
-    float Y[K][K], E[K][K], R[K][K], D[K][K];
-#pragma unroll
-    for (int i = 0; i < K; ++i)
-#pragma unroll
-        for (int j = 0; j < K; ++j) {
-            Y[i][j] = Y0[i][j] * sc;
-            E[i][j] = E0[i][j] * sc;
-            R[i][j] = (i == j) ? 1.f : 0.f;
-            D[i][j] = 0.f;
-        }
-    for (int k = 12; k >= 1; --k) {
-        const float r = 1.f / (float)k;
-        float nR[K][K], nD[K][K];
-#pragma unroll
-        for (int i = 0; i < K; ++i)
-#pragma unroll
-            for (int j = 0; j < K; ++j) {
-                float a = 0.f, b = 0.f;
-#pragma unroll
-                for (int m = 0; m < K; ++m) {
-                    a = fmaf(Y[i][m], R[m][j], a);
-                    b = fmaf(E[i][m], R[m][j], fmaf(Y[i][m], D[m][j], b));
-                }
-                nR[i][j] = fmaf(a, r, (i == j) ? 1.f : 0.f);
-                nD[i][j] = b * r;
-            }
-#pragma unroll
-        for (int i = 0; i < K; ++i)
-#pragma unroll
-            for (int j = 0; j < K; ++j) { R[i][j] = nR[i][j]; D[i][j] = nD[i][j]; }
-    }
-    for (int s = 0; s < sq; ++s) {
-        float nR[K][K], nD[K][K];
-#pragma unroll
-        for (int i = 0; i < K; ++i)
-#pragma unroll
-            for (int j = 0; j < K; ++j) {
-                float a = 0.f, b = 0.f;
-#pragma unroll
-                for (int m = 0; m < K; ++m) {
-                    a = fmaf(R[i][m], R[m][j], a);
-                    b = fmaf(D[i][m], R[m][j], fmaf(R[i][m], D[m][j], b));
-                }
-                nR[i][j] = a;
-                nD[i][j] = b;
-            }
-#pragma unroll
-        for (int i = 0; i < K; ++i)
-#pragma unroll
-            for (int j = 0; j < K; ++j) { R[i][j] = nR[i][j]; D[i][j] = nD[i][j]; }
-    }
-#pragma unroll
-    for (int i = 0; i < K; ++i)
-#pragma unroll
-        for (int j = 0; j < K; ++j) L[i][j] = D[i][j];
-}
-
 template <int N, int MODE>
 __global__ void __launch_bounds__(256)
     k_finalize(int nC, Steps st, const float *__restrict__ partials, int parts,
@@ -281,61 +206,7 @@ __global__ void __launch_bounds__(256)
         g[i] = s;
     }
     __syncthreads();
-    if constexpr (MODE == 0) {
-        // S_c = sum_n lambda_{n+1} [p_n;1]^T  ->
-        // G_c = h S_c (I + h/2 [A_c;0])^T + h^2/2 A_lin^T S_c
-        for (int c = tid; c < nC; c += B) {
-            const float *a = A + ((long long)th * nC + c) * P;
-            float S[N][N + 1], Gc[N][N + 1];
-#pragma unroll
-            for (int i = 0; i < N; ++i)
-#pragma unroll
-                for (int j = 0; j <= N; ++j) S[i][j] = g[c * P + i * (N + 1) + j];
-#pragma unroll
-            for (int i = 0; i < N; ++i)
-#pragma unroll
-                for (int j = 0; j <= N; ++j) {
-                    float x = 0.f, y = 0.f;
-                    if (j < N) {
-#pragma unroll
-                        for (int k = 0; k <= N; ++k) x = fmaf(S[i][k], a[j * (N + 1) + k], x);
-                    }
-#pragma unroll
-                    for (int r = 0; r < N; ++r) y = fmaf(a[r * (N + 1) + i], S[r][j], y);
-                    Gc[i][j] = fmaf(st.h, fmaf(st.hh, x, S[i][j]), st.hh2 * y);
-                }
-#pragma unroll
-            for (int i = 0; i < N; ++i)
-#pragma unroll
-                for (int j = 0; j <= N; ++j) g[c * P + i * (N + 1) + j] = Gc[i][j];
-        }
-        __syncthreads();
-    } else {
-        const float dt = st.h;
-        // dL/dT_c (top N rows) -> dL/dA_c = dt * [L_exp(X^T, [dL/dT_c; 0])]_{top rows}
-        for (int c = tid; c < nC; c += B) {
-            const float *a = A + ((long long)th * nC + c) * P;
-            float Y[N + 1][N + 1], E[N + 1][N + 1], L[N + 1][N + 1];
-#pragma unroll
-            for (int i = 0; i <= N; ++i)
-#pragma unroll
-                for (int j = 0; j <= N; ++j) {
-                    Y[j][i] = (i < N) ? dt * a[i * (N + 1) + j] : 0.f;   // Y = X^T
-                    E[i][j] = (i < N) ? g[c * P + i * (N + 1) + j] : 0.f;
-                }
-            frechet_expm<N + 1>(Y, E, L);
-#pragma unroll
-            for (int i = 0; i < N; ++i)
-#pragma unroll
-                for (int j = 0; j <= N; ++j) g[c * P + i * (N + 1) + j] = dt * L[i][j];
-        }
-        __syncthreads();
-    }
-    for (int k = tid; k < d; k += B) {
-        float acc = 0.f;
-        for (int i = 0; i < G; ++i) acc = fmaf(__ldg(basis + (long long)i * d + k), g[i], acc);
-        dtheta[(long long)th * d + k] = acc;
-    }
+    finish_theta<N, MODE>(g, A + (long long)th * G, nC, st, basis, d, dtheta + (long long)th * d);
 }
 
 cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *partials, int parts,

@@ -7,10 +7,6 @@
 namespace cpab {
 
 constexpr int kSeg = 10;
-// Flush queue: entries per warp, and the row stride of its value array (odd,
-// so that the draining lanes, one per component, hit distinct banks).
-constexpr int kQueue = 40;
-constexpr int kQueueStride = kQueue + 1;
 
 struct Steps {
     float h, hh, hh2;   // 1/N, 1/(2N), 1/(2N^2)
@@ -45,12 +41,14 @@ __host__ __device__ constexpr int dtab_stride() { return N == 1 ? 1 : (N == 2 ? 
 // Per-cell propagator of the adjoint, D with lambda_n = lambda_{n+1} + D^T lambda_{n+1}:
 //   mode 0: D = h A_lin + h^2/2 A_lin^2  (M - I of the midpoint sensitivity)
 //   mode 1: D = E_lin                     (the linear part of T - I)
-// stored row-major, D[r][k] at dtab[c * stride + r * N + k].  Written by the
-// whole block; the caller synchronises.
+// stored row-major, D[r][k] at dtab[c * stride + r * N + k].  Cells are
+// split over the calling threads (first, first + stride, ...); the caller
+// synchronises.
 template <int N, int MODE>
-__device__ __forceinline__ void build_dtab(const float *tab, float *dtab, int nC, const Steps &st) {
+__device__ __forceinline__ void build_dtab(const float *tab, float *dtab, int nC, const Steps &st,
+                                           int first, int stride) {
     constexpr int P = N * (N + 1);
-    for (int c = threadIdx.x; c < nC; c += blockDim.x) {
+    for (int c = first; c < nC; c += stride) {
         const float *a = tab + c * P;
         float *d = dtab + c * dtab_stride<N>();
 #pragma unroll
@@ -121,8 +119,6 @@ __host__ __device__ inline int round4(int x) { return (x + 3) & ~3; }
 //   tab   [round4(G)]            cell table of this theta (TMA destination)
 //   dtab  [round4(nC*stride)]    per-cell adjoint propagators D
 //   gw    [W][round4(G)]         per-warp cell-gradient tables
-//   qv    [W][P][kQueueStride]   per-warp flush queue, values
-//   qc    [W][kQueue] (int)      per-warp flush queue, cells
 //   ck    [nseg][N][block]       checkpoints (position every kSeg steps)
 //   pb    [kSeg][N][block]       positions of the segment being reversed
 //   cl    [nsteps][block] (CT)   per-step cells
@@ -136,15 +132,14 @@ __host__ __device__ inline size_t adjoint_smem_bytes(int nC, int nsteps, int blo
     const int W = block / 32;
     const int nseg = (nsteps + kSeg - 1) / kSeg;
     size_t b = (size_t)G * 4 + (size_t)Dn * 4 + (size_t)W * G * 4 +
-               (size_t)W * (P * kQueueStride + kQueue) * 4 + (size_t)nseg * N * block * 4 +
-               (size_t)kSeg * N * block * 4 + (size_t)nsteps * block * sizeof(CT);
+               (size_t)nseg * N * block * 4 + (size_t)kSeg * N * block * 4 +
+               (size_t)nsteps * block * sizeof(CT);
     return (b + 15) & ~(size_t)15;
 }
 
 template <int N, typename CT>
 struct AdjSmem {
-    float *tab, *dtab, *gw, *qv, *ck, *pb;
-    int *qc;
+    float *tab, *dtab, *gw, *ck, *pb;
     CT *cl;
 };
 
@@ -158,54 +153,89 @@ __device__ __forceinline__ AdjSmem<N, CT> carve_adjoint(float *base, int nC, int
     s.tab = base;
     s.dtab = s.tab + Gr;
     s.gw = s.dtab + round4(nC * dtab_stride<N>());
-    s.qv = s.gw + (size_t)W * Gr;
-    s.qc = reinterpret_cast<int *>(s.qv + (size_t)W * P * kQueueStride);
-    s.ck = reinterpret_cast<float *>(s.qc + (size_t)W * kQueue);
+    s.ck = s.gw + (size_t)W * Gr;
     s.pb = s.ck + (size_t)nseg * N * B;
     s.cl = reinterpret_cast<CT *>(s.pb + (size_t)kSeg * N * B);
     return s;
 }
 
-// Per-warp flush queue.  A lane that leaves a cell appends (cell, S) in the
-// order (step, lane); when fewer than 32 free entries remain the warp adds
-// the entries into its cell-gradient table in queue order (one lane per
-// component), so the sums are reproducible.  `n` is warp-uniform.
+// Sum each contiguous lane run [lo, hi] of sum[] into lane lo (five fixed
+// shuffle rounds) and add it there.  All lanes of m call it; runs lie in m.
 template <int P>
-struct FlushQueue {
-    float *qv;   // [P][kQueueStride]
-    int *qc;     // [kQueue]
-    float *tab;  // warp's cell-gradient table
-    int n;
-};
-
-template <int P>
-__device__ __forceinline__ void queue_drain(FlushQueue<P> &q) {
-    __syncwarp();
+__device__ __forceinline__ void add_runs(unsigned m, int lo, int hi, float (&sum)[P], float *dst) {
     const int lane = threadIdx.x & 31;
-    if (lane < P) {
-        const float *src = q.qv + lane * kQueueStride;
-        float *dst = q.tab + lane;
-#pragma unroll 1
-        for (int e = 0; e < q.n; ++e) dst[q.qc[e] * P] += src[e];
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+            const float u = __shfl_down_sync(m, sum[i], off);
+            if (lane + off <= hi) sum[i] += u;
+        }
     }
-    __syncwarp();
-    q.n = 0;
+    if (lane == lo) {
+#pragma unroll
+        for (int i = 0; i < P; ++i) dst[i] += sum[i];
+    }
 }
 
-// Append the accumulators of the lanes in m (warp-uniform mask; called by all
-// lanes of the warp).
+// Add the accumulators of the lanes in m (the lanes leaving a cell at this
+// step; called by exactly those lanes) into the warp's cell table.  Lanes that
+// leave the same cell at the same step are first summed into their lowest
+// lane (a fixed shuffle tree when every group is a contiguous run of more than
+// four lanes, else a lane-order chain), so every table element receives at
+// most one add per step, in step order, and the summation order depends only
+// on the inputs: the sums are reproducible.  In the common case (no two lanes
+// share a cell) all lanes add in one pass.
 template <int P>
-__device__ __forceinline__ void queue_push(FlushQueue<P> &q, unsigned m, int cell,
-                                           const float (&acc)[P]) {
+__device__ __forceinline__ void flush_cells(unsigned m, int cell, const float (&acc)[P],
+                                            float *warp_tab) {
     const int lane = threadIdx.x & 31;
-    if ((m >> lane) & 1u) {
-        const int e = q.n + __popc(m & ((1u << lane) - 1u));
+    float *dst = warp_tab + cell * P;
+    const unsigned grp = __match_any_sync(m, cell);
+    const unsigned gmax = __reduce_max_sync(m, (unsigned)__popc(grp));
+    if (gmax == 1u) {
 #pragma unroll
-        for (int i = 0; i < P; ++i) q.qv[i * kQueueStride + e] = acc[i];
-        q.qc[e] = cell;
+        for (int i = 0; i < P; ++i) dst[i] += acc[i];
+        return;
     }
-    q.n += __popc(m);
-    if (q.n > kQueue - 32) queue_drain<P>(q);
+    float sum[P];
+#pragma unroll
+    for (int i = 0; i < P; ++i) sum[i] = acc[i];
+    const int lo = __ffs(grp) - 1;
+    const unsigned run = grp >> lo;
+    if (gmax > 4u && __all_sync(m, (run & (run + 1u)) == 0u)) {
+        // Every group is a contiguous run of lanes [lo, hi] (typical when
+        // neighbouring points cross a face together): tree reduction towards
+        // the lowest lane in five fixed shuffle rounds.
+        add_runs<P>(m, lo, 31 - __clz(grp), sum, dst);
+        return;
+    }
+    unsigned rest = grp & (grp - 1u);        // the other members, lowest first
+    for (unsigned k = 1; k < gmax; ++k) {
+        const int src = rest ? __ffs(rest) - 1 : lane;
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+            const float u = __shfl_sync(m, acc[i], src);
+            if (rest) sum[i] += u;
+        }
+        rest &= rest - 1u;
+    }
+    if (lane == __ffs(grp) - 1) {
+#pragma unroll
+        for (int i = 0; i < P; ++i) dst[i] += sum[i];
+    }
+}
+
+// Warp-level flush: lanes with flush = true add their accumulators for
+// `cell`.  Called by all lanes of the warp.
+template <int P>
+__device__ __forceinline__ void warp_flush(bool flush, int cell, const float (&acc)[P],
+                                           float *warp_tab) {
+    const unsigned m = __ballot_sync(0xffffffffu, flush);
+    if (m) {
+        if (flush) flush_cells<P>(m, cell, acc, warp_tab);
+        __syncwarp();
+    }
 }
 
 // Reverse sweep of one trajectory whose cells are logged in cl and whose
@@ -217,7 +247,7 @@ __device__ __forceinline__ void queue_push(FlushQueue<P> &q, unsigned m, int cel
 template <int N, int MODE, typename CT>
 __device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nsteps,
                                               const Steps &st, bool live, float (&lam)[N],
-                                              FlushQueue<N * (N + 1)> &q) {
+                                              float *warp_tab) {
     constexpr int P = N * (N + 1);
     const int B = blockDim.x, tid = threadIdx.x;
     const int nseg = (nsteps + kSeg - 1) / kSeg;
@@ -241,8 +271,7 @@ __device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nste
         for (int s = len - 1; s >= 0; --s) {
             const int c = (int)sm.cl[(n0 + s) * B + tid];
             const bool change = c != gcell;
-            const unsigned m = __ballot_sync(0xffffffffu, change && gcell >= 0 && live);
-            if (m) queue_push<P>(q, m, gcell, acc);
+            warp_flush<P>(change && gcell >= 0 && live, gcell, acc, warp_tab);
             if (change) {
                 gcell = c;
 #pragma unroll
@@ -254,8 +283,7 @@ __device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nste
             adjoint_step<N>(sm.dtab, c, p, lam, acc);
         }
     }
-    const unsigned m = __ballot_sync(0xffffffffu, gcell >= 0 && live);
-    if (m) queue_push<P>(q, m, gcell, acc);
+    warp_flush<P>(gcell >= 0 && live, gcell, acc, warp_tab);
 }
 
 // Forward sweep that logs cells and checkpoints; p holds p_0 on entry and
@@ -289,37 +317,166 @@ __device__ __forceinline__ bool adjoint_prologue(const AdjSmem<N, CT> &sm, const
     constexpr int P = N * (N + 1);
     const int W = blockDim.x / 32, Gr = round4(nC * P);
     if (!stage_table(sm.tab, table, nC * P, bar, err)) return false;
-    build_dtab<N, MODE>(sm.tab, sm.dtab, nC, st);
+    build_dtab<N, MODE>(sm.tab, sm.dtab, nC, st, threadIdx.x, blockDim.x);
     for (int i = threadIdx.x; i < W * Gr; i += blockDim.x) sm.gw[i] = 0.f;
     __syncthreads();
     return true;
 }
 
+// Kernel epilogue: write this CTA's partial (per-warp tables summed in warp
+// order).
 template <int N, typename CT>
-__device__ __forceinline__ FlushQueue<N * (N + 1)> warp_queue(const AdjSmem<N, CT> &sm, int nC) {
-    constexpr int P = N * (N + 1);
-    const int w = threadIdx.x >> 5;
-    FlushQueue<P> q;
-    q.qv = sm.qv + (size_t)w * P * kQueueStride;
-    q.qc = sm.qc + (size_t)w * kQueue;
-    q.tab = sm.gw + (size_t)w * round4(nC * P);
-    q.n = 0;
-    return q;
-}
-
-// Kernel epilogue: drain every warp's queue, then write this CTA's partial
-// (per-warp tables summed in warp order).
-template <int N, typename CT>
-__device__ __forceinline__ void adjoint_epilogue(const AdjSmem<N, CT> &sm, FlushQueue<N * (N + 1)> &q,
-                                                 int nC, float *dst) {
+__device__ __forceinline__ void adjoint_epilogue(const AdjSmem<N, CT> &sm, int nC, float *dst) {
     constexpr int P = N * (N + 1);
     const int B = blockDim.x, W = B / 32, G = nC * P, Gr = round4(G);
-    queue_drain<P>(q);
     __syncthreads();
     for (int i = threadIdx.x; i < G; i += B) {
         float s = 0.f;
         for (int w = 0; w < W; ++w) s += sm.gw[(size_t)w * Gr + i];
         dst[i] = s;
+    }
+}
+
+// Frechet derivative of expm at Y in direction E, by a truncated Horner
+// recursion on Y/2^s, E/2^s followed by s squarings:
+//   R_{k-1} = I + (Y/k) R_k,  dR_{k-1} = (E/k) R_k + (Y/k) dR_k,
+//   then  L <- L R + R L,  R <- R R.
+template <int K>
+__device__ __forceinline__ void frechet_expm(const float (&Y0)[K][K], const float (&E0)[K][K],
+                                             float (&L)[K][K]) {
+    float norm = 0.f;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        float s = 0.f;
+#pragma unroll
+        for (int i = 0; i < K; ++i) s += fabsf(Y0[i][j]);
+        norm = fmaxf(norm, s);
+    }
+    int sq = 0;
+    if (norm > 0.5f) sq = min(64, (int)ceilf(log2f(norm / 0.5f)));
+    const float sc = ldexpf(1.f, -sq);
+    float Y[K][K], E[K][K], R[K][K], D[K][K];
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            Y[i][j] = Y0[i][j] * sc;
+            E[i][j] = E0[i][j] * sc;
+            R[i][j] = (i == j) ? 1.f : 0.f;
+            D[i][j] = 0.f;
+        }
+    for (int k = 12; k >= 1; --k) {
+        const float r = 1.f / (float)k;
+        float nR[K][K], nD[K][K];
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                float a = 0.f, b = 0.f;
+#pragma unroll
+                for (int m = 0; m < K; ++m) {
+                    a = fmaf(Y[i][m], R[m][j], a);
+                    b = fmaf(E[i][m], R[m][j], fmaf(Y[i][m], D[m][j], b));
+                }
+                nR[i][j] = fmaf(a, r, (i == j) ? 1.f : 0.f);
+                nD[i][j] = b * r;
+            }
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = 0; j < K; ++j) { R[i][j] = nR[i][j]; D[i][j] = nD[i][j]; }
+    }
+    for (int s = 0; s < sq; ++s) {
+        float nR[K][K], nD[K][K];
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                float a = 0.f, b = 0.f;
+#pragma unroll
+                for (int m = 0; m < K; ++m) {
+                    a = fmaf(R[i][m], R[m][j], a);
+                    b = fmaf(D[i][m], R[m][j], fmaf(R[i][m], D[m][j], b));
+                }
+                nR[i][j] = a;
+                nD[i][j] = b;
+            }
+#pragma unroll
+        for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = 0; j < K; ++j) { R[i][j] = nR[i][j]; D[i][j] = nD[i][j]; }
+    }
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+#pragma unroll
+        for (int j = 0; j < K; ++j) L[i][j] = D[i][j];
+}
+
+// Per-theta tail of the finalize kernels, run by one block after the summed
+// cell statistics are in g (shared memory, nC * N*(N+1) floats): map them to
+// dL/dA (mode 0: G = h S (I + h/2 [A;0])^T + h^2/2 A_lin^T S; mode 1: adjoint
+// Frechet derivative of expm) and contract with the basis,
+// dtheta[k] = sum_i B[i, k] dA[i].
+template <int N, int MODE>
+__device__ __forceinline__ void finish_theta(float *g, const float *__restrict__ A_th, int nC,
+                                             const Steps &st, const float *__restrict__ basis,
+                                             int d, float *__restrict__ dth) {
+    constexpr int P = N * (N + 1);
+    const int tid = threadIdx.x, B = blockDim.x, G = nC * P;
+    if constexpr (MODE == 0) {
+        // S_c = sum_n lambda_{n+1} [p_n;1]^T  ->
+        // G_c = h S_c (I + h/2 [A_c;0])^T + h^2/2 A_lin^T S_c
+        for (int c = tid; c < nC; c += B) {
+            const float *a = A_th + (long long)c * P;
+            float S[N][N + 1], Gc[N][N + 1];
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+#pragma unroll
+                for (int j = 0; j <= N; ++j) S[i][j] = g[c * P + i * (N + 1) + j];
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+#pragma unroll
+                for (int j = 0; j <= N; ++j) {
+                    float x = 0.f, y = 0.f;
+                    if (j < N) {
+#pragma unroll
+                        for (int k = 0; k <= N; ++k) x = fmaf(S[i][k], a[j * (N + 1) + k], x);
+                    }
+#pragma unroll
+                    for (int r = 0; r < N; ++r) y = fmaf(a[r * (N + 1) + i], S[r][j], y);
+                    Gc[i][j] = fmaf(st.h, fmaf(st.hh, x, S[i][j]), st.hh2 * y);
+                }
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+#pragma unroll
+                for (int j = 0; j <= N; ++j) g[c * P + i * (N + 1) + j] = Gc[i][j];
+        }
+        __syncthreads();
+    } else {
+        const float dt = st.h;
+        // dL/dT_c (top N rows) -> dL/dA_c = dt * [L_exp(X^T, [dL/dT_c; 0])]_{top rows}
+        for (int c = tid; c < nC; c += B) {
+            const float *a = A_th + (long long)c * P;
+            float Y[N + 1][N + 1], E[N + 1][N + 1], L[N + 1][N + 1];
+#pragma unroll
+            for (int i = 0; i <= N; ++i)
+#pragma unroll
+                for (int j = 0; j <= N; ++j) {
+                    Y[j][i] = (i < N) ? dt * a[i * (N + 1) + j] : 0.f;   // Y = X^T
+                    E[i][j] = (i < N) ? g[c * P + i * (N + 1) + j] : 0.f;
+                }
+            frechet_expm<N + 1>(Y, E, L);
+#pragma unroll
+            for (int i = 0; i < N; ++i)
+#pragma unroll
+                for (int j = 0; j <= N; ++j) g[c * P + i * (N + 1) + j] = dt * L[i][j];
+        }
+        __syncthreads();
+    }
+    for (int k = tid; k < d; k += B) {
+        float acc = 0.f;
+        for (int i = 0; i < G; ++i) acc = fmaf(__ldg(basis + (long long)i * d + k), g[i], acc);
+        dth[k] = acc;
     }
 }
 

@@ -374,6 +374,244 @@ int cpab_device_status(unsigned *flags, int clear) {
 
 }  // extern "C"
 
+// ------------------------- ragged batched 1D series -------------------------
+namespace {
+
+// Kinds of ragged kernels with their own launch shape (autotuner key).
+constexpr int kRaggedForward = 0, kRaggedAdjoint = 1;
+
+// Launch shape: the autotuned one for this problem if cpab_ragged1d_tune ran
+// on it, else the defaults (forward: 256 threads, 2 points per lane;
+// adjoint: the largest block whose shared memory fits, 1 pass per tile).
+bool ragged_shape(int kind, int mode, const Tess &t, int nsteps, int S, long long total,
+                  int *block, int *ppt) {
+    if (ragged_get_tuned(kind, mode, t, nsteps, S, total, block, ppt)) return true;
+    if (kind == kRaggedForward) {
+        *block = 256;
+        *ppt = 2;
+        return true;
+    }
+    *ppt = 1;
+    const int cands[3] = {256, 128, 64};
+    for (int i = 0; i < 3; ++i)
+        if (ragged_adjoint_smem_for(t, nsteps, mode, cands[i])) {
+            *block = cands[i];
+            return true;
+        }
+    return false;
+}
+
+int check_ragged(int nc, int nsteps, int S, long long total, const long long *offsets, Tess *t) {
+    int rc = make_tess(1, &nc, t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if (S < 0 || total < 0) return fail(CPAB_ERR_ARGUMENT, "need S >= 0 and total >= 0");
+    // warp tiles are counted in 32-bit integers (at most 128 points per tile)
+    if (total + (long long)S * 128 >= (1ll << 31))
+        return fail(CPAB_ERR_UNSUPPORTED, "total + 128 * S must be below 2^31");
+    if (S > 0 && !offsets) return fail(CPAB_ERR_ARGUMENT, "offsets is NULL");
+    return CPAB_OK;
+}
+
+int check_ragged_ws(const Tess &t, int S, void *workspace, size_t workspace_bytes) {
+    const size_t need = ragged_workspace_bytes(t, S);
+    if (!workspace || workspace_bytes < need)
+        return fail(CPAB_ERR_WORKSPACE, "workspace of %zu bytes needed (got %zu)", need,
+                    workspace ? workspace_bytes : (size_t)0);
+    return CPAB_OK;
+}
+
+int ragged_adjoint_run(const Tess &t, int nsteps, int mode, bool fused, int block, int ppt,
+                       int S, const long long *offsets, long long total, RaggedBwd a,
+                       const float *basis, int d, float *dtheta, float *sse, void *ws,
+                       unsigned long long *ties, cudaStream_t s) {
+    if (a.dvalues && total > 0) {
+        cudaError_t e = cudaMemsetAsync(a.dvalues, 0, (size_t)total * sizeof(float), s);
+        if (e != cudaSuccess) return cuda_fail(e, "memset");
+    }
+    cudaError_t e = launch_ragged_adjoint(t, nsteps, mode, fused, block, ppt, S, offsets, total,
+                                          a, basis, d, d > 0 ? dtheta : nullptr, sse, ws, ties,
+                                          device_error_word(), s);
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "ragged adjoint launch");
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t cpab_ragged1d_workspace(int nc, int nsteps, int S) {
+    g_err[0] = 0;
+    Tess t;
+    if (make_tess(1, &nc, &t) || check_steps(nsteps)) return 0;
+    if (S < 0) {
+        fail(CPAB_ERR_ARGUMENT, "need S >= 0");
+        return 0;
+    }
+    return ragged_workspace_bytes(t, S);
+}
+
+int cpab_ragged1d_forward(int nc, int nsteps, const float *E, int S, const long long *offsets,
+                          long long total, const float *values, float *out, void *workspace,
+                          size_t workspace_bytes, unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = check_ragged(nc, nsteps, S, total, offsets, &t);
+    if (rc) return rc;
+    if (S == 0 || total == 0) return CPAB_OK;
+    if (!E || !values || !out) return fail(CPAB_ERR_ARGUMENT, "E, values or out is NULL");
+    if ((rc = check_ragged_ws(t, S, workspace, workspace_bytes))) return rc;
+    int block, ppt;
+    ragged_shape(kRaggedForward, 0, t, nsteps, S, total, &block, &ppt);
+    cudaError_t e = launch_ragged_forward(t, nsteps, block, ppt, S, offsets, total, E, values, out,
+                                          workspace, ties, device_error_word(), as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "ragged forward launch");
+}
+
+int cpab_ragged1d_backward(int nc, int nsteps, int mode, const float *A, const float *E, int S,
+                           const long long *offsets, long long total, const float *basis, int d,
+                           const float *values, const float *grad_out, float *dtheta,
+                           float *dvalues, void *workspace, size_t workspace_bytes,
+                           unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = check_ragged(nc, nsteps, S, total, offsets, &t);
+    if (rc) return rc;
+    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+        return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
+    if (d < 0) return fail(CPAB_ERR_ARGUMENT, "negative d");
+    if (S == 0) return CPAB_OK;
+    if (!A || !E || (total > 0 && (!values || !grad_out)) || (d > 0 && (!basis || !dtheta)))
+        return fail(CPAB_ERR_ARGUMENT, "A, E, values, grad_out, basis or dtheta is NULL");
+    if ((rc = check_ragged_ws(t, S, workspace, workspace_bytes))) return rc;
+    int block, ppt;
+    if (!ragged_shape(kRaggedAdjoint, mode, t, nsteps, S, total, &block, &ppt))
+        return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
+    RaggedBwd a = {};
+    a.A = A;
+    a.E = E;
+    a.values = values;
+    a.gout = grad_out;
+    a.dvalues = dvalues;
+    return ragged_adjoint_run(t, nsteps, mode, false, block, ppt, S, offsets, total, a, basis, d,
+                              dtheta, nullptr, workspace, ties, as_stream(stream));
+}
+
+int cpab_ragged1d_mse(int nc, int nsteps, int mode, const float *A, const float *E, int S,
+                      const long long *offsets, long long total, const float *basis, int d,
+                      const float *values, const float *target, float loss_scale, float *out,
+                      float *sse, float *dtheta, float *dvalues, void *workspace,
+                      size_t workspace_bytes, unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = check_ragged(nc, nsteps, S, total, offsets, &t);
+    if (rc) return rc;
+    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+        return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
+    if (d < 0) return fail(CPAB_ERR_ARGUMENT, "negative d");
+    if (S == 0) return CPAB_OK;
+    if (!A || !E || !sse || (total > 0 && (!values || !target)) || (d > 0 && (!basis || !dtheta)))
+        return fail(CPAB_ERR_ARGUMENT, "A, E, values, target, sse, basis or dtheta is NULL");
+    if ((rc = check_ragged_ws(t, S, workspace, workspace_bytes))) return rc;
+    int block, ppt;
+    if (!ragged_shape(kRaggedAdjoint, mode, t, nsteps, S, total, &block, &ppt))
+        return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
+    RaggedBwd a = {};
+    a.A = A;
+    a.E = E;
+    a.values = values;
+    a.target = target;
+    a.loss_scale = loss_scale;
+    a.out = out;
+    a.dvalues = dvalues;
+    return ragged_adjoint_run(t, nsteps, mode, true, block, ppt, S, offsets, total, a, basis, d,
+                              dtheta, sse, workspace, ties, as_stream(stream));
+}
+
+int cpab_ragged1d_tune(int kind, int nc, int nsteps, int mode, const float *A, const float *E,
+                       int S, const long long *offsets, long long total, const float *basis,
+                       int d, const float *values, const float *target, float loss_scale,
+                       float *out, float *sse, float *dtheta, float *dvalues, void *workspace,
+                       size_t workspace_bytes, int *shape, float *best_ms, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = check_ragged(nc, nsteps, S, total, offsets, &t);
+    if (rc) return rc;
+    if (kind != kRaggedForward && kind != kRaggedAdjoint)
+        return fail(CPAB_ERR_ARGUMENT, "kind must be 0 (forward) or 1 (adjoint)");
+    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+        return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
+    if (S == 0 || total == 0) return fail(CPAB_ERR_ARGUMENT, "nothing to tune (no points)");
+    if (!E || !values || !out || (kind == kRaggedAdjoint &&
+                                  (!A || !target || !sse || (d > 0 && (!basis || !dtheta)))))
+        return fail(CPAB_ERR_ARGUMENT, "a required pointer is NULL");
+    if ((rc = check_ragged_ws(t, S, workspace, workspace_bytes))) return rc;
+    cudaStream_t s = as_stream(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone)
+        return fail(CPAB_ERR_ARGUMENT, "cpab_ragged1d_tune times launches; call it outside capture");
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        return cuda_fail(cudaGetLastError(), "event create");
+    RaggedBwd a = {};
+    a.A = A;
+    a.E = E;
+    a.values = values;
+    a.target = target;
+    a.loss_scale = loss_scale;
+    a.out = out;
+    a.dvalues = dvalues;
+    unsigned *err = device_error_word();
+    auto run = [&](int block, int ppt) -> int {
+        if (kind == kRaggedForward) {
+            cudaError_t e = launch_ragged_forward(t, nsteps, block, ppt, S, offsets, total, E,
+                                                  values, out, workspace, nullptr, err, s);
+            return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "ragged forward launch");
+        }
+        return ragged_adjoint_run(t, nsteps, mode, true, block, ppt, S, offsets, total, a, basis,
+                                  d, dtheta, sse, workspace, nullptr, s);
+    };
+    const int blocks[3] = {64, 128, 256};
+    const int ppts[3] = {1, 2, 4};
+    float best = 3.0e38f;
+    int bb = 0, bp = 0;
+    for (int bi = 0; bi < 3 && rc == CPAB_OK; ++bi) {
+        if (kind == kRaggedAdjoint && !ragged_adjoint_smem_for(t, nsteps, mode, blocks[bi]))
+            continue;
+        for (int pi = 0; pi < 3 && rc == CPAB_OK; ++pi) {
+            if ((rc = run(blocks[bi], ppts[pi]))) break;   // warm-up
+            float ms = 3.0e38f;
+            for (int rep = 0; rep < 3 && rc == CPAB_OK; ++rep) {
+                cudaEventRecord(e0, s);
+                rc = run(blocks[bi], ppts[pi]);
+                cudaEventRecord(e1, s);
+                cudaError_t e = cudaEventSynchronize(e1);
+                if (e != cudaSuccess) rc = cuda_fail(e, "tuning run");
+                float m = 0.f;
+                cudaEventElapsedTime(&m, e0, e1);
+                if (m < ms) ms = m;
+            }
+            if (rc == CPAB_OK && ms < best) {
+                best = ms;
+                bb = blocks[bi];
+                bp = ppts[pi];
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (!bb) return fail(CPAB_ERR_UNSUPPORTED, "no launch shape fits this tessellation");
+    ragged_set_tuned(kind, mode, t, nsteps, S, total, bb, bp);
+    if (shape) {
+        shape[0] = bb;
+        shape[1] = bp;
+    }
+    if (best_ms) *best_ms = best;
+    return run(bb, bp);   // leave the outputs of the chosen shape
+}
+
+}  // extern "C"
+
 // --------------------------------------------------------------------------
 // cpab_backward without a caller-provided workspace.
 //

@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(256)
 
     const int b = blockIdx.y, part = blockIdx.x;
     if (!adjoint_prologue<N, MODE, CT>(sm, table + (long long)b * G, t.nC, st, &bar, err)) return;
-    auto q = warp_queue<N, CT>(sm, t.nC);
+    float *warp_tab = sm.gw + (size_t)(tid >> 5) * round4(G);
 
     for (int tile = part; tile < tiles; tile += parts) {
         const int o = tile * B + tid;
@@ -175,9 +175,9 @@ __global__ void __launch_bounds__(256)
         }
 #pragma unroll
         for (int r = 0; r < N; ++r) lam[r] = gf[r] * (float)(g.size[r] - 1);
-        reverse_sweep<N, MODE, CT>(sm, nsteps, st, live, lam, q);
+        reverse_sweep<N, MODE, CT>(sm, nsteps, st, live, lam, warp_tab);
     }
-    adjoint_epilogue<N, CT>(sm, q, t.nC, partials + ((long long)b * parts + part) * G);
+    adjoint_epilogue<N, CT>(sm, t.nC, partials + ((long long)b * parts + part) * G);
 }
 
 template <int N, int MODE, typename CT>

@@ -86,6 +86,42 @@ cudaError_t launch_transform_data_backward(const Tess &t, int nsteps, int mode,
                                            unsigned long long *ties, unsigned *err,
                                            cudaStream_t s);
 
+// Ragged batched 1D series (cpab_ragged.cu).  Series s has the points
+// torch.linspace(0, 1, L_s) and the values values[off[s] .. off[s+1]).
+constexpr long long kRaggedMaxLen = 1ll << 22;   // per-series length limit
+
+struct RaggedBwd;
+size_t ragged_workspace_bytes(const Tess &t, int S);
+size_t ragged_adjoint_smem_for(const Tess &t, int nsteps, int mode, int block);
+bool ragged_get_tuned(int kind, int mode, const Tess &t, int nsteps, int S, long long total,
+                      int *block, int *ppt);
+void ragged_set_tuned(int kind, int mode, const Tess &t, int nsteps, int S, long long total,
+                      int block, int ppt);
+cudaError_t launch_ragged_forward(const Tess &t, int nsteps, int block, int ppt, int S,
+                                  const long long *off, long long total, const float *E,
+                                  const float *values, float *out, void *ws,
+                                  unsigned long long *ties, unsigned *err, cudaStream_t s);
+
+struct RaggedBwd {
+    const float *A;        // [S][nC][2]   (mode 0 trajectory table, finalize)
+    const float *E;        // [S][nC][2]
+    const float *values;   // [total]
+    const float *target;   // [total] (fused MSE) or null
+    const float *gout;     // [total] (plain backward) or null
+    float loss_scale;      // fused MSE: dL/d(out) = loss_scale * (out - target)
+    float *out;            // [total] (fused MSE, optional)
+    float *dvalues;        // [total] (optional, accumulated)
+    float *partials;       // [(TW + S)][nC * 2]  (set from the workspace)
+    float *sse_partials;   // [(TW + S)]          (set from the workspace)
+};
+// fused = true: dL/d(out) from the MSE residual against `target`, per-series
+// sum of squared residuals into sse[S]; fused = false: dL/d(out) = gout.
+cudaError_t launch_ragged_adjoint(const Tess &t, int nsteps, int mode, bool fused, int block,
+                                  int ppt, int S, const long long *off, long long total,
+                                  const RaggedBwd &a, const float *basis, int d, float *dtheta,
+                                  float *sse, void *ws, unsigned long long *ties, unsigned *err,
+                                  cudaStream_t s);
+
 int num_sms();
 
 }  // namespace cpab

@@ -12,7 +12,8 @@ from __future__ import annotations
 import torch
 
 from . import _native as N
-from ._autograd import TransformGrid, TransformGridNumeric, Interpolate, TransformData
+from ._autograd import (TransformGrid, TransformGridNumeric, Interpolate, TransformData,
+                        TransformDataRagged)
 
 
 # ---------------------------------------------------------------- utilities --
@@ -181,6 +182,48 @@ def transform_data(data, theta, params, outsize):
                                 data.device)
         return interpolate(params.ndim, data, transformer(grid, theta, params), outsize)
     return TransformData.apply(data, theta, params, outsize)
+
+
+def _check_ragged(values, offsets, theta, params):
+    _require_cuda(values, offsets, theta)
+    if params.ndim != 1:
+        raise ValueError('ragged series need a 1D tessellation')
+    if values.dim() != 1:
+        raise ValueError('values must be 1D: all series concatenated')
+    if offsets.dim() != 1 or offsets.dtype != torch.int64:
+        raise ValueError('offsets must be a 1D int64 tensor of n_series + 1 entries')
+    if theta.dim() != 2 or theta.shape[0] != offsets.numel() - 1:
+        raise ValueError('theta must be [n_series=%d, d]' % (offsets.numel() - 1))
+
+
+def transform_data_ragged(values, offsets, theta, params):
+    """Ragged batch of 1D series: series s is values[offsets[s]:offsets[s+1]]
+    and is warped by theta[s] exactly as transform_data(values_s[None, None],
+    theta[s:s+1], params, [L_s]) would (libcpab/cpab.py:304-331), all series
+    in one launch.  Returns the warped values, concatenated like values."""
+    _check_ragged(values, offsets, theta, params)
+    return TransformDataRagged.apply(values, theta, offsets.contiguous(), params)
+
+
+def ragged_mse(values, target, offsets, theta, params, loss_scale=None, want_out=False,
+               want_dvalues=True, workspace=None):
+    """Fused forward + squared-error loss + backward for ragged 1D series.
+    Returns a dict: loss (scalar tensor, loss_scale/2 * sum of squared
+    residuals; the mean squared error by default), sse [n_series], dtheta
+    [n_series, d], dvalues (or None) and out (or None)."""
+    _check_ragged(values, offsets, theta, params)
+    from ._autograd import _mode, _ties
+    basis = basis_on(params, values.device)
+    A, _, E = N.cell_tables(params.nc, params.nstepsolver,
+                            theta.detach().to(torch.float32).contiguous(), basis)
+    if loss_scale is None:
+        loss_scale = 2.0 / max(values.numel(), 1)
+    res = N.ragged_mse(params.nc, params.nstepsolver, _mode(params), A, E, offsets.contiguous(),
+                       values.detach().contiguous(), target.detach().contiguous(), basis,
+                       loss_scale=loss_scale, want_out=want_out, want_dvalues=want_dvalues,
+                       ties=_ties(params), workspace=workspace)
+    res['loss'] = res['sse'].sum() * (0.5 * loss_scale)
+    return res
 
 
 def findcellidx(ndim, p, nc):

@@ -182,6 +182,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_capi_argument_errors_without_gpu():
     """Argument validation runs before any device work."""
+    import ctypes
     from libcpab_gb300 import _native as N
     lib = N.load()
     assert lib.cpab_num_cells(2, N._ints([3, 3])) == 36
@@ -193,6 +194,17 @@ def test_capi_argument_errors_without_gpu():
     rc = lib.cpab_backward(2, N._ints([3, 3]), 50, 7, None, 0, 10, None, None, 1, None, 34,
                            None, None, None, None, 0, None, None)
     assert rc == 1 and b'mode' in lib.cpab_last_error()
+    rc = lib.cpab_ragged1d_forward(0, 50, None, 1, None, 10, None, None, None, 0, None, None)
+    assert rc == 1 and b'nc' in lib.cpab_last_error()
+    rc = lib.cpab_ragged1d_mse(10, 50, 0, None, None, -1, None, 0, None, 10, None, None, 1.0,
+                               None, None, None, None, None, 0, None, None)
+    assert rc == 1 and b'S >= 0' in lib.cpab_last_error()
+    rc = lib.cpab_ragged1d_backward(10, 50, 5, None, None, 1, ctypes.c_void_p(16), 10, None, 10,
+                                    None, None, None, None, None, 0, None, None)
+    assert rc == 1 and b'mode' in lib.cpab_last_error()
+    rc = lib.cpab_ragged1d_mse(10, 50, 0, None, None, 4, None, 0, None, 10, None, None, 1.0,
+                               None, None, None, None, None, 0, None, None)
+    assert rc == 1 and b'offsets' in lib.cpab_last_error()
 
 
 # -------------------------------------------------------------- host API --
