@@ -51,8 +51,9 @@ def parse():
                     help='images per step (the headline workload uses 64; smaller values '
                          'are for profiling runs only)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
-    ap.add_argument('--no-ragged', action='store_true',
-                    help='skip the ragged 1D series leg (reported beside the headline)')
+    ap.add_argument('--no-extra', action='store_true',
+                    help='skip the workloads reported beside the headline (ragged 1D '
+                         'series, 3D volume warp, interpolator sweep)')
     args = ap.parse_args()
     return args
 
@@ -253,7 +254,10 @@ def run_gb300(args):
     for _ in range(2):
         step_unfused()
     t_unf = time_events(step_unfused, args.steps, flush)
-    ragged = run_ragged(device, args.steps, flush) if rank == 0 and not args.no_ragged else None
+    extra = rank == 0 and not args.no_extra
+    ragged = run_ragged(device, args.steps, flush) if extra else None
+    volume = run_volume(device, args.steps, flush) if extra else None
+    interp = run_interp_sweep(device, args.steps, flush) if extra else None
     clk = clocks.stop() if clocks else None
     status = N.device_status()
 
@@ -305,6 +309,8 @@ def run_gb300(args):
                             'value': pts / (sum(t_unf) / len(t_unf) / 1e3),
                             'unit': 'points/s'},
             'ragged_1d': ragged,
+            'volume_3d': volume,
+            'interpolate_2d': interp,
             'clocks': clk, 'device_status': status,
         }
     if world > 1:
@@ -385,6 +391,100 @@ def run_ragged(device, steps, flush):
             'launches_per_step': 4, 'tuned_shape_fused': list(shape_b),
             'tuned_shape_forward': list(shape_f), 'forward_only_ms': ms_f,
             'loss': loss}
+
+
+def hbm_peak():
+    """Measured copy bandwidth of this GPU model (GB/s), else the fallback."""
+    try:
+        with open(os.path.join(HERE, 'MEASURED_PEAKS.json')) as f:
+            return float(json.load(f)['hbm_gbs']), 'measured (MEASURED_PEAKS.json hbm_gbs)'
+    except (OSError, ValueError, KeyError):
+        return 6800.0, 'fallback'
+
+
+def make_volumes(device, nb=8, size=128, blobs=32, seed=1):
+    """[nb, 1, size^3] volumes, each a sum of `blobs` isotropic Gaussian blobs
+    (centres uniform in the volume, sigma ~ U[2, 8] voxels, amplitude ~
+    U[0.5, 1])."""
+    g = torch.Generator().manual_seed(seed)
+    centres = (torch.rand(nb, blobs, 3, generator=g) * size).to(device)
+    sigma = (2 + 6 * torch.rand(nb, blobs, generator=g)).to(device)
+    amp = (0.5 + 0.5 * torch.rand(nb, blobs, generator=g)).to(device)
+    ax = torch.arange(size, dtype=torch.float32, device=device)
+    f = torch.exp(-(ax[None, None, None, :] - centres[..., None]) ** 2
+                  / (2 * sigma[..., None, None] ** 2))               # [nb, blobs, 3, size]
+    vol = torch.einsum('nb,nbx,nby,nbz->nxyz', amp, f[:, :, 0], f[:, :, 1], f[:, :, 2])
+    return vol[:, None].contiguous()
+
+
+def run_volume(device, steps, flush):
+    """3D volume warp: tess [4,4,4] zero_boundary + volume_perservation, 8 theta
+    ~ N(0, I), [8, 1, 128^3] blob volumes, MSE against the volumes warped by a
+    second theta; fused forward + dtheta/d(data) backward through the public
+    API.  Also the trilinear interpolator alone (HBM-bound)."""
+    from libcpab_gb300 import Cpab, _native as N
+    T = Cpab([4, 4, 4], backend='pytorch', device='gpu', zero_boundary=True,
+             volume_perservation=True)
+    d = T.get_theta_dim()
+    theta = torch.randn(8, d, generator=torch.Generator().manual_seed(0)).to(device)
+    theta2 = torch.randn(8, d, generator=torch.Generator().manual_seed(2)).to(device)
+    data = make_volumes(device)
+    osz = [128, 128, 128]
+    with torch.no_grad():
+        target = T.transform_data(data, theta2, osz)
+
+    def step():
+        th = theta.detach().requires_grad_(True)
+        dd = data.detach().requires_grad_(True)
+        loss = F.mse_loss(T.transform_data(dd, th, osz), target)
+        loss.backward()
+        return loss
+    for _ in range(3):
+        step()
+    t_step = time_events(step, steps, flush)
+    grid = T.transform_grid(T.uniform_meshgrid(osz), theta)
+    for _ in range(3):
+        N.interpolate(data, grid, osz)
+    t_int = time_events(lambda: N.interpolate(data, grid, osz), steps, flush)
+    pts = 8 * 128 ** 3
+    ms, ms_i = sum(t_step) / len(t_step), sum(t_int) / len(t_int)
+    peak, src = hbm_peak()
+    gbs = pts * 20 / (ms_i / 1e3) / 1e9     # data read + output write 8 B (C = 1), grid 12 B
+    return {'workload': 'transform_data 3D tess [4,4,4] zero_boundary volume_perservation, 8 '
+                        'theta ~ N(0,I), [8,1,128^3] Gaussian-blob volumes, MSE, fwd + '
+                        'dtheta/d(data) bwd (reference gradient)',
+            'value': pts / (ms / 1e3), 'unit': 'points/s', 'ms_per_step': ms,
+            'interpolate': {'ms': ms_i, 'algorithmic_bytes': pts * 20, 'gbs': gbs,
+                            'frac_of_hbm': gbs / peak, 'peak_gbs': peak, 'peak_source': src}}
+
+
+def run_interp_sweep(device, steps, flush):
+    """Bilinear interpolator alone (cpab_interpolate) on [nb, 3, 224, 224] with
+    CPAB-warped grids (tess [3,3], theta ~ N(0, 0.25 I)).  Algorithmic bytes
+    per output point: 8 C (data read once, output written once) + 4 ndim (the
+    grid, an input of the standalone op), against the measured HBM
+    bandwidth."""
+    from libcpab_gb300 import Cpab, _native as N
+    peak, src = hbm_peak()
+    T = Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True)
+    mesh = T.uniform_meshgrid([SIZE, SIZE])
+    res = []
+    for nb in (64, 256, 1024):
+        g = torch.Generator(device=device).manual_seed(nb)
+        data = torch.rand(nb, 3, SIZE, SIZE, device=device, generator=g)
+        th = THETA_STD * torch.randn(nb, T.get_theta_dim(), device=device, generator=g)
+        with torch.no_grad():
+            grid = T.transform_grid(mesh, th)
+        for _ in range(3):
+            N.interpolate(data, grid, [SIZE, SIZE])
+        t = time_events(lambda: N.interpolate(data, grid, [SIZE, SIZE]), steps, flush)
+        ms = sum(t) / len(t)
+        nbytes = nb * SIZE * SIZE * (8 * 3 + 4 * 2)
+        gbs = nbytes / (ms / 1e3) / 1e9
+        res.append({'n_batch': nb, 'ms': ms, 'algorithmic_bytes': nbytes, 'gbs': gbs,
+                    'frac_of_hbm': gbs / peak})
+        del data, grid
+    return {'sweep': res, 'peak_gbs': peak, 'peak_source': src}
 
 
 def cpu_reference_step(sample, orc, T_h, nc):

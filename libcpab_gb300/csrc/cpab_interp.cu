@@ -8,7 +8,15 @@
 // [nb, C, W_out(, H_out(, D_out))].  The reference builds ~30 launches of
 // int64 index tensors and gathers (plus a host-built batch index that is
 // copied to the device on every call); here one thread handles one output
-// point for all channels.  Grid: x over points of an image, y over images.
+// point for all channels.
+//
+// Memory order: the grid is meshgrid-ordered (x fastest) while data and
+// output have the last axis fastest.  In 2D/3D a block therefore takes a
+// 32 x 32 tile of (x, last axis) points (at one y in 3D), reads the tile's
+// grid coordinates coalesced along x into shared memory, and then works in
+// output order (last axis across the lanes): the output stores are
+// contiguous and neighbouring lanes gather neighbouring data elements.  The
+// backward writes d(grid) back through the same tile.  1D needs no tiling.
 //
 // Backward: d(data) is a scatter-add (float atomics into a zeroed buffer, like
 // the reference's autograd index_put accumulation); d(grid) follows the
@@ -67,6 +75,147 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// --------------------------- tiled 2D / 3D kernels ---------------------------
+constexpr int kTile = 32, kRows = 8;   // 32 x 32 tile, 256 threads
+
+// Tile t of an image: a = x index (grid-fast), z = last-axis index
+// (output-fast), mid = y index in 3D (0 in 2D).
+struct TileGeo {
+    int ta, tz;   // tiles along x and along the last axis
+};
+
+template <int N>
+__device__ __forceinline__ void tile_coords(const Geo &g, const TileGeo &tg, int t, int &a0,
+                                            int &z0, int &mid) {
+    const int per = tg.ta * tg.tz;
+    mid = (N == 3) ? t / per : 0;
+    const int r = t - mid * per;
+    a0 = (r % tg.ta) * kTile;
+    z0 = (r / tg.ta) * kTile;
+}
+
+// meshgrid index of (x = a, y = mid, last = z) and output offset
+template <int N>
+__device__ __forceinline__ int grid_index(const Geo &g, int a, int mid, int z) {
+    if constexpr (N == 2) return a + g.outsize[0] * z;
+    else return a + g.outsize[0] * (mid + g.outsize[1] * z);
+}
+template <int N>
+__device__ __forceinline__ int out_index(const Geo &g, int a, int mid, int z) {
+    if constexpr (N == 2) return a * g.outsize[1] + z;
+    else return (a * g.outsize[1] + mid) * g.outsize[2] + z;
+}
+
+// Stage the tile's grid coordinates: sp[j][z_local][a_local].
+template <int N>
+__device__ __forceinline__ void load_grid_tile(const Geo &g, const float *gb, int a0, int z0,
+                                               int mid, float (*sp)[kTile][kTile + 1]) {
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int A = g.outsize[0], Z = g.outsize[N - 1];
+#pragma unroll
+    for (int r = 0; r < kTile / kRows; ++r) {
+        const int zl = ty + kRows * r, a = a0 + tx, z = z0 + zl;
+        if (a < A && z < Z) {
+            const int k = grid_index<N>(g, a, mid, z);
+#pragma unroll
+            for (int j = 0; j < N; ++j) sp[j][zl][tx] = __ldg(gb + (long long)j * g.nP + k);
+        }
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256)
+    k_interpolate_tiled(Geo g, TileGeo tg, const float *__restrict__ data, int C,
+                        const float *__restrict__ grid, float *__restrict__ out, int nb) {
+    __shared__ float sp[N][kTile][kTile + 1];
+    int a0, z0, mid;
+    tile_coords<N>(g, tg, blockIdx.x, a0, z0, mid);
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int A = g.outsize[0], Z = g.outsize[N - 1];
+    for (int b = blockIdx.y; b < nb; b += gridDim.y) {
+        __syncthreads();
+        load_grid_tile<N>(g, grid + (long long)b * N * g.nP, a0, z0, mid, sp);
+        __syncthreads();
+#pragma unroll 1
+        for (int r = 0; r < kTile / kRows; ++r) {
+            const int al = ty + kRows * r, a = a0 + al, z = z0 + tx;
+            if (a >= A || z >= Z) continue;
+            float p[N];
+#pragma unroll
+            for (int j = 0; j < N; ++j) p[j] = sp[j][tx][al];
+            const Corner<N> cr = corners<N>(p, g);
+            const int o = out_index<N>(g, a, mid, z);
+            for (int c = 0; c < C; ++c) {
+                const long long plane = (long long)b * C + c;
+                out[plane * g.nP + o] = lerp_corners<N>(data + plane * g.nD, cr);
+            }
+        }
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256)
+    k_interpolate_backward_tiled(Geo g, TileGeo tg, const float *__restrict__ data, int C,
+                                 const float *__restrict__ grid, const float *__restrict__ gout,
+                                 float *__restrict__ ddata, float *__restrict__ dgrid, int nb) {
+    __shared__ float sp[N][kTile][kTile + 1];
+    int a0, z0, mid;
+    tile_coords<N>(g, tg, blockIdx.x, a0, z0, mid);
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int A = g.outsize[0], Z = g.outsize[N - 1];
+    for (int b = blockIdx.y; b < nb; b += gridDim.y) {
+        __syncthreads();
+        load_grid_tile<N>(g, grid + (long long)b * N * g.nP, a0, z0, mid, sp);
+        __syncthreads();
+        float gfs[kTile / kRows][N];
+#pragma unroll
+        for (int r = 0; r < kTile / kRows; ++r) {
+            const int al = ty + kRows * r, a = a0 + al, z = z0 + tx;
+#pragma unroll
+            for (int j = 0; j < N; ++j) gfs[r][j] = 0.f;
+            if (a >= A || z >= Z) continue;
+            float p[N];
+#pragma unroll
+            for (int j = 0; j < N; ++j) p[j] = sp[j][tx][al];
+            const Corner<N> cr = corners<N>(p, g);
+            const int o = out_index<N>(g, a, mid, z);
+            for (int c = 0; c < C; ++c) {
+                const long long plane = (long long)b * C + c;
+                const float w = __ldg(gout + plane * g.nP + o);
+                lerp_grads<N>(data + plane * g.nD, cr, w, ddata ? ddata + plane * g.nD : nullptr,
+                              gfs[r]);
+            }
+        }
+        if (!dgrid) continue;
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kTile / kRows; ++r) {
+            const int al = ty + kRows * r;
+#pragma unroll
+            for (int j = 0; j < N; ++j) sp[j][tx][al] = gfs[r][j] * g.sizem1[j];
+        }
+        __syncthreads();
+        float *db = dgrid + (long long)b * N * g.nP;
+#pragma unroll
+        for (int r = 0; r < kTile / kRows; ++r) {
+            const int zl = ty + kRows * r, a = a0 + tx, z = z0 + zl;
+            if (a < A && z < Z) {
+                const int k = grid_index<N>(g, a, mid, z);
+#pragma unroll
+                for (int j = 0; j < N; ++j) db[(long long)j * g.nP + k] = sp[j][zl][tx];
+            }
+        }
+    }
+}
+
+static TileGeo make_tiles(int ndim, const Geo &g, unsigned *blocks) {
+    TileGeo tg;
+    tg.ta = (g.outsize[0] + kTile - 1) / kTile;
+    tg.tz = (g.outsize[ndim - 1] + kTile - 1) / kTile;
+    *blocks = (unsigned)tg.ta * tg.tz * (ndim == 3 ? (unsigned)g.outsize[1] : 1u);
+    return tg;
+}
+
 cudaError_t launch_interpolate(int ndim, const float *data, int nb, int C, const int *size,
                                const float *grid, const int *outsize, float *out,
                                cudaStream_t s) {
@@ -75,11 +224,15 @@ cudaError_t launch_interpolate(int ndim, const float *data, int nb, int C, const
     const int block = 256;
     const dim3 gridn((unsigned)((g.nP + block - 1) / block),
                      (unsigned)(nb < (int)kMaxGridY ? nb : kMaxGridY));
-    switch (ndim) {
-        case 1: k_interpolate<1><<<gridn, block, 0, s>>>(g, data, C, grid, out, nb); break;
-        case 2: k_interpolate<2><<<gridn, block, 0, s>>>(g, data, C, grid, out, nb); break;
-        default: k_interpolate<3><<<gridn, block, 0, s>>>(g, data, C, grid, out, nb); break;
+    if (ndim == 1) {
+        k_interpolate<1><<<gridn, block, 0, s>>>(g, data, C, grid, out, nb);
+        return cudaGetLastError();
     }
+    unsigned blocks = 0;
+    const TileGeo tg = make_tiles(ndim, g, &blocks);
+    const dim3 tgrid(blocks, gridn.y);
+    if (ndim == 2) k_interpolate_tiled<2><<<tgrid, block, 0, s>>>(g, tg, data, C, grid, out, nb);
+    else k_interpolate_tiled<3><<<tgrid, block, 0, s>>>(g, tg, data, C, grid, out, nb);
     return cudaGetLastError();
 }
 
@@ -92,11 +245,19 @@ cudaError_t launch_interpolate_backward(int ndim, const float *data, int nb, int
     const int block = 256;
     const dim3 gridn((unsigned)((g.nP + block - 1) / block),
                      (unsigned)(nb < (int)kMaxGridY ? nb : kMaxGridY));
-    switch (ndim) {
-        case 1: k_interpolate_backward<1><<<gridn, block, 0, s>>>(g, data, C, grid, gout, ddata, dgrid, nb); break;
-        case 2: k_interpolate_backward<2><<<gridn, block, 0, s>>>(g, data, C, grid, gout, ddata, dgrid, nb); break;
-        default: k_interpolate_backward<3><<<gridn, block, 0, s>>>(g, data, C, grid, gout, ddata, dgrid, nb); break;
+    if (ndim == 1) {
+        k_interpolate_backward<1><<<gridn, block, 0, s>>>(g, data, C, grid, gout, ddata, dgrid, nb);
+        return cudaGetLastError();
     }
+    unsigned blocks = 0;
+    const TileGeo tg = make_tiles(ndim, g, &blocks);
+    const dim3 tgrid(blocks, gridn.y);
+    if (ndim == 2)
+        k_interpolate_backward_tiled<2><<<tgrid, block, 0, s>>>(g, tg, data, C, grid, gout, ddata,
+                                                               dgrid, nb);
+    else
+        k_interpolate_backward_tiled<3><<<tgrid, block, 0, s>>>(g, tg, data, C, grid, gout, ddata,
+                                                               dgrid, nb);
     return cudaGetLastError();
 }
 
