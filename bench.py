@@ -51,6 +51,11 @@ def parse():
                     help='images per step (the headline workload uses 64; smaller values '
                          'are for profiling runs only)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--leg', default='all', choices=['all', 'ragged', 'volume', 'interp'],
+                    help='run only one of the side workloads and print its result (for '
+                         'profiling runs)')
+    ap.add_argument('--no-tune', action='store_true',
+                    help='ragged leg: use the default launch shapes instead of autotuning')
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the workloads reported beside the headline (ragged 1D '
                          'series, 3D volume warp, interpolator sweep)')
@@ -255,7 +260,7 @@ def run_gb300(args):
         step_unfused()
     t_unf = time_events(step_unfused, args.steps, flush)
     extra = rank == 0 and not args.no_extra
-    ragged = run_ragged(device, args.steps, flush) if extra else None
+    ragged = run_ragged(device, args.steps, flush, tune=not args.no_tune) if extra else None
     volume = run_volume(device, args.steps, flush) if extra else None
     interp = run_interp_sweep(device, args.steps, flush) if extra else None
     clk = clocks.stop() if clocks else None
@@ -351,7 +356,7 @@ def ragged_inputs(T, device):
     return theta.to(device), off, values, target, basis
 
 
-def run_ragged(device, steps, flush):
+def run_ragged(device, steps, flush, tune=True):
     """Fused forward + MSE + dtheta/d(values) adjoint of the ragged workload in
     one persistent launch (plus the tile-prefix and finalize kernels and the
     cell tables), autotuned, captured in a CUDA graph and replayed."""
@@ -361,10 +366,12 @@ def run_ragged(device, steps, flush):
     total = values.numel()
     A, _, E = N.cell_tables([RAGGED_NC], NSTEPS, theta, basis)
     ws = N.ragged_workspace(RAGGED_NC, NSTEPS, RAGGED_S, device)
-    shape_f, ms_f, _ = N.ragged_tune(0, [RAGGED_NC], NSTEPS, 0, A, E, off, values, target, basis,
-                                     workspace=ws)
-    shape_b, ms_b, _ = N.ragged_tune(1, [RAGGED_NC], NSTEPS, 0, A, E, off, values, target, basis,
-                                     workspace=ws)
+    shape_f = shape_b = ms_f = None
+    if tune:
+        shape_f, ms_f, _ = N.ragged_tune(0, [RAGGED_NC], NSTEPS, 0, A, E, off, values, target,
+                                         basis, workspace=ws)
+        shape_b, _, _ = N.ragged_tune(1, [RAGGED_NC], NSTEPS, 0, A, E, off, values, target,
+                                      basis, workspace=ws)
     st = torch.cuda.Stream()
     st.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(st):
@@ -388,8 +395,9 @@ def run_ragged(device, steps, flush):
                         'gradient) in one persistent launch, CUDA-graph replay'
                         % (RAGGED_S, RAGGED_LEN[0], RAGGED_LEN[1], total, RAGGED_NC),
             'value': total / (ms / 1e3), 'unit': 'points/s', 'ms_per_step': ms,
-            'launches_per_step': 4, 'tuned_shape_fused': list(shape_b),
-            'tuned_shape_forward': list(shape_f), 'forward_only_ms': ms_f,
+            'launches_per_step': 4, 'tuned_shape_fused': list(shape_b) if shape_b else None,
+            'tuned_shape_forward': list(shape_f) if shape_f else None,
+            'forward_only_ms': ms_f,
             'loss': loss}
 
 
@@ -569,6 +577,16 @@ def main():
                 'e2e': {'value': v, 'unit': 'points/s', 'h2d_bytes_per_step': 0,
                         'd2h_bytes_per_step': 0}}
         print(json.dumps(line))
+        return
+    if args.leg != 'all':
+        device = torch.device('cuda', 0)
+        torch.cuda.set_device(device)
+        flush_buf = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=device)
+        flush = lambda: flush_buf.fill_(1.0)
+        fn = {'ragged': lambda: run_ragged(device, args.steps, flush, tune=not args.no_tune),
+              'volume': lambda: run_volume(device, args.steps, flush),
+              'interp': lambda: run_interp_sweep(device, args.steps, flush)}[args.leg]
+        print(json.dumps({'leg': args.leg, 'result': fn()}))
         return
     res = run_gb300(args)
     if rank == 0 and res is not None:

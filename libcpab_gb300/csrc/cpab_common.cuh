@@ -310,12 +310,25 @@ static CPAB_HD __noinline__ int cell_3d_exact(float p0, float p1, float p2, cons
 }
 
 CPAB_HD inline int cell_3d_fast(float p0, float p1, float p2, const Tess &t) {
-    // With x and y in [0,1] the push-inside rule does not apply; the
-    // reference then clamps each coordinate to [0, clamp3] (in float) and
-    // splits it, which split_exact does exactly.  Only the tetrahedron plane
-    // tests need a margin.
+    // The reference's push-inside rule (x or y outside [0,1]) is float
+    // arithmetic: it is applied here with the same operations, and leaves
+    // every coordinate in [0,1].  The reference then clamps each coordinate to
+    // [0, clamp3] (in float) and splits it, which split_exact does exactly.
+    // Only the tetrahedron plane tests need a margin.
     if (!(fabsf(p0) <= 1e30f) || !(fabsf(p1) <= 1e30f) || !(fabsf(p2) <= 1e30f)) return -1;
-    if (p0 >= 0.f && p0 <= 1.f && p1 >= 0.f && p1 <= 1.f) {
+    if (!(p0 >= 0.f && p0 <= 1.f && p1 >= 0.f && p1 <= 1.f)) {
+        const float h = 0.5f;
+        p0 = CPAB_SUB_RN(p0, h); p1 = CPAB_SUB_RN(p1, h); p2 = CPAB_SUB_RN(p2, h);
+        const float a0 = fabsf(p0), a1 = fabsf(p1), a2 = fabsf(p2);
+        const float s0 = (a0 < a1 && a0 < a2) ? CPAB_MUL_RN(h, t.inc[0]) : 0.0f;
+        const float s1 = (a1 < a0 && a0 < a2) ? CPAB_MUL_RN(h, t.inc[1]) : 0.0f;
+        const float s2 = (a2 < a0 && a0 < a1) ? CPAB_MUL_RN(h, t.inc[2]) : 0.0f;
+        if (a0 > h) p0 = copysignf(CPAB_SUB_RN(h, s0), p0);
+        if (a1 > h) p1 = copysignf(CPAB_SUB_RN(h, s1), p1);
+        if (a2 > h) p2 = copysignf(CPAB_SUB_RN(h, s2), p2);
+        p0 = CPAB_ADD_RN(p0, h); p1 = CPAB_ADD_RN(p1, h); p2 = CPAB_ADD_RN(p2, h);
+    }
+    {
         const float c0 = (p0 < t.clamp3[0]) ? p0 : t.clamp3[0];
         const float c1 = (p1 < t.clamp3[1]) ? p1 : t.clamp3[1];
         float c2 = (0.f < p2) ? p2 : 0.f;

@@ -52,23 +52,27 @@ def grid512():
     return np.stack([gx.reshape(-1), gy.reshape(-1)]).astype(np.float32)
 
 
-def evaluate(theta, pts, cuda, oracle, grad=True, seed=1):
-    """GPU vs FP64 oracle on theta [n, d] and points [2, nP]; returns a dict of
-    error statistics (and asserts nothing)."""
+def evaluate(theta, pts, cuda, oracle, grad=True, seed=1, nc=None, B=None):
+    """GPU vs FP64 oracle on theta [n, d] and points [ndim, nP] (default: the
+    [8,8] free tessellation); returns a dict of error statistics (and asserts
+    nothing)."""
     from libcpab_gb300 import _native as N
     from libcpab_gb300.tessellation import make_tessellation
     from oracle.oracle import numpy_transform_grid, fp64_autograd
-    B = make_tessellation(NC, False, False).B
+    nc = NC if nc is None else list(nc)
+    ndim = len(nc)
+    if B is None:
+        B = make_tessellation(nc, False, False).B
     basis = torch.tensor(np.ascontiguousarray(B), dtype=torch.float32, device=cuda)
     th = torch.tensor(theta, device=cuda)
-    A, T, E = N.cell_tables(NC, NSTEPS, th, basis, want_T=True)
+    A, T, E = N.cell_tables(nc, NSTEPS, th, basis, want_T=True)
     P = torch.tensor(pts, device=cuda)
     ties = torch.zeros(1, dtype=torch.int64, device=cuda)
-    out = N.integrate(NC, NSTEPS, P, E, ties=ties)
-    out_t, cells = N.integrate_trace(NC, NSTEPS, P, E)
+    out = N.integrate(nc, NSTEPS, P, E, ties=ties)
+    out_t, cells = N.integrate_trace(nc, NSTEPS, P, E)
     assert torch.equal(out, out_t)
     out, cells = out.cpu().numpy(), cells.cpu().numpy()
-    ref, cells64, marg = numpy_transform_grid(B, theta, pts, NC, NSTEPS, return_cells=True,
+    ref, cells64, marg = numpy_transform_grid(B, theta, pts, nc, NSTEPS, return_cells=True,
                                               return_margin='steps', semantics='cpp')
     diff = cells != cells64
     tie = diff.any(axis=2)
@@ -77,7 +81,7 @@ def evaluate(theta, pts, cuda, oracle, grad=True, seed=1):
     ti, pi = np.nonzero(tie)
     first_margin = marg[ti, pi, first[ti, pi]] if ti.size else np.zeros(0)
     # the reference's own fp32 scheme (p <- T p~) on the same points, for comparison
-    ref32 = oracle.forward(NC, NSTEPS, pts, T.cpu().numpy())
+    ref32 = oracle.forward(nc, NSTEPS, pts, T.cpu().numpy())
     err32 = np.abs(ref32 - ref).max(axis=1)
     scale = np.maximum(1.0, np.abs(ref).max(axis=1))          # points far outside: fp32 ulps
     away = marg.min(axis=2) >= 1e-4                           # never near a decision boundary
@@ -97,11 +101,11 @@ def evaluate(theta, pts, cuda, oracle, grad=True, seed=1):
         gen = np.random.default_rng(seed)
         cot = gen.standard_normal(out.shape).astype(np.float32)
         cot_d = torch.tensor(cot, device=cuda)
-        d0, _ = N.backward(NC, NSTEPS, 0, P, A, E, basis, cot_d)
-        d1, _ = N.backward(NC, NSTEPS, 1, P, A, E, basis, cot_d)
-        Bs = B.T.reshape(B.shape[1], -1, 2, 3).astype(np.float32)
-        ref0 = oracle.backward(NC, NSTEPS, pts, A.cpu().numpy(), Bs, cot)
-        _, ref1, _ = fp64_autograd(B, theta, pts, NC, cot, NSTEPS, cells=cells)
+        d0, _ = N.backward(nc, NSTEPS, 0, P, A, E, basis, cot_d)
+        d1, _ = N.backward(nc, NSTEPS, 1, P, A, E, basis, cot_d)
+        Bs = B.T.reshape(B.shape[1], -1, ndim, ndim + 1).astype(np.float32)
+        ref0 = oracle.backward(nc, NSTEPS, pts, A.cpu().numpy(), Bs, cot)
+        _, ref1, _ = fp64_autograd(B, theta, pts, nc, cot, NSTEPS, cells=cells)
         rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
         r['dtheta_rel_err_reference_mode'] = rel(d0.cpu().numpy(), ref0)
         r['dtheta_rel_err_exact_mode'] = rel(d1.cpu().numpy(), ref1)
@@ -110,8 +114,8 @@ def evaluate(theta, pts, cuda, oracle, grad=True, seed=1):
         # comparison restricted to trajectories that stay >= 1e-4 from every
         # decision boundary (FP64)
         cot_away = (cot * away[:, None, :]).astype(np.float32)
-        d0a, _ = N.backward(NC, NSTEPS, 0, P, A, E, basis, torch.tensor(cot_away, device=cuda))
-        ref0a = oracle.backward(NC, NSTEPS, pts, A.cpu().numpy(), Bs, cot_away)
+        d0a, _ = N.backward(nc, NSTEPS, 0, P, A, E, basis, torch.tensor(cot_away, device=cuda))
+        ref0a = oracle.backward(nc, NSTEPS, pts, A.cpu().numpy(), Bs, cot_away)
         r['dtheta_rel_err_reference_mode_off_boundary'] = rel(d0a.cpu().numpy(), ref0a)
     return r
 
@@ -157,6 +161,41 @@ def test_precision_stress_full_grid_runs(cuda):
     assert N.device_status() == 0
 
 
+def other_configs(cuda, orc):
+    """Error against the FP64 oracle for the other workloads' distributions,
+    on their grids (sampled where large)."""
+    from conftest import load_golden
+    from libcpab_gb300.tessellation import make_tessellation
+    from libcpab_gb300.functions import uniform_meshgrid
+    rep = {}
+    rng = np.random.default_rng(3)
+
+    def theta_of(B, n, std, seed):
+        g = torch.Generator().manual_seed(seed)
+        return (std * torch.randn(n, B.shape[1], generator=g)).numpy().astype(np.float32)
+
+    def sample(mesh, n):
+        idx = np.sort(rng.choice(mesh.shape[1], size=min(n, mesh.shape[1]), replace=False))
+        return np.ascontiguousarray(mesh[:, idx])
+    B1 = make_tessellation([50], True, False).B
+    m1 = uniform_meshgrid(1, [0], [1], [1000]).numpy()
+    rep['cfg1 1D [50] zb, 16 theta ~ N(0,I), 1000-point grid'] = evaluate(
+        theta_of(B1, 16, 1.0, 0), m1, cuda, orc, nc=[50], B=B1)
+    B2 = make_tessellation([3, 3], True, False).B
+    m2 = uniform_meshgrid(2, [0, 0], [1, 1], [224, 224]).numpy()
+    rep['cfg2 2D [3,3] zb, 64 theta ~ N(0,0.25I), 4096 of the 224^2 grid points'] = evaluate(
+        theta_of(B2, 64, 0.5, 0), sample(m2, 4096), cuda, orc, nc=[3, 3], B=B2)
+    B3 = make_tessellation([100], False, False).B
+    m3 = np.linspace(0, 1, 4096, dtype=np.float32)[None]
+    rep['cfg3 1D [100] free, 64 theta ~ N(0,I), 4096-point series grid'] = evaluate(
+        theta_of(B3, 64, 1.0, 0), m3, cuda, orc, nc=[100], B=B3)
+    B4 = load_golden('L_3d_4x4x4_zb_vp')['B']
+    m4 = uniform_meshgrid(3, [0, 0, 0], [1, 1, 1], [128] * 3).numpy()
+    rep['cfg4 3D [4,4,4] zb vp, 8 theta ~ N(0,I), 4096 of the 128^3 grid points'] = evaluate(
+        theta_of(B4, 8, 1.0, 0), sample(m4, 4096), cuda, orc, nc=[4, 4, 4], B=B4)
+    return rep
+
+
 def main():
     from libcpab_gb300.tessellation import make_tessellation
     from oracle.oracle import Oracle
@@ -170,6 +209,7 @@ def main():
                         'sampled grid points'}
     report['large'] = evaluate(theta[:32], pts, cuda, orc)
     report['near_identity'] = evaluate(theta[256:288], pts, cuda, orc)
+    report['other_configs'] = other_configs(cuda, orc)
     # GPU-only: FP64 tie lookups over the whole configuration
     from libcpab_gb300 import _native as N
     B = make_tessellation(NC, False, False).B
