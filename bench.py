@@ -38,6 +38,10 @@ L2_BYTES = 129 * 2 ** 20
 # algorithmic work per point trajectory (2D, 50 steps): forward 17 flop/step,
 # adjoint 37 flop/step; interpolation 8*C bytes (forward), 12*C (backward)
 FLOP_FWD_STEP, FLOP_ADJ_STEP = 17, 37
+# DRAM bytes (read + write) of one k_transform_data_backward launch per image,
+# from an ncu capture of 16 images (35.64 MB); traffic grows with the images
+# processed
+BWD_DRAM_BYTES_PER_IMAGE = 35.64e6 / 16
 
 
 def parse():
@@ -302,7 +306,9 @@ def run_gb300(args):
                          'peak_source': 'derived: 152 SM x 128 FP32 lanes x 2 flop x 2070 MHz '
                                         '(MEASURED_PEAKS has HBM and bf16 only)',
                          'flop_per_launch': bwd_flop, 'ms_per_launch': bwd_ms,
-                         'traffic': None},
+                         'traffic': BWD_DRAM_BYTES_PER_IMAGE * args.batch,
+                         'traffic_unit': 'bytes per launch (ncu dram read+write, 16-image '
+                                         'capture scaled by images)'},
             'forward_kernel': {'name': 'k_transform_data', 'ms_per_launch': fwd_ms,
                                'flop_per_launch': pts * NSTEPS * FLOP_FWD_STEP,
                                'tflops': pts * NSTEPS * FLOP_FWD_STEP / (fwd_ms / 1e3) / 1e12,
