@@ -201,12 +201,21 @@ __global__ void __launch_bounds__(256)
     const int G = nC * P;
     const float *src = partials + (long long)th * parts * G;
     for (int i = tid; i < G; i += B) {
-        float s = 0.f;
-        for (int q = 0; q < parts; ++q) s += __ldg(src + (long long)q * G + i);
-        g[i] = s;
+        // four interleaved sums (loads in flight), combined in a fixed order
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+        int q = 0;
+        for (; q + 4 <= parts; q += 4) {
+            s0 += __ldg(src + (long long)q * G + i);
+            s1 += __ldg(src + (long long)(q + 1) * G + i);
+            s2 += __ldg(src + (long long)(q + 2) * G + i);
+            s3 += __ldg(src + (long long)(q + 3) * G + i);
+        }
+        for (; q < parts; ++q) s0 += __ldg(src + (long long)q * G + i);
+        g[i] = (s0 + s1) + (s2 + s3);
     }
     __syncthreads();
-    finish_theta<N, MODE>(g, A + (long long)th * G, nC, st, basis, d, dtheta + (long long)th * d);
+    finish_theta<N, MODE>(g, g + round4(G), A + (long long)th * G, nC, st, basis, d,
+                          dtheta + (long long)th * d);
 }
 
 cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *partials, int parts,
@@ -214,12 +223,12 @@ cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *pa
                             float *dtheta, cudaStream_t s) {
     if (n_theta == 0) return cudaSuccess;
     const int P = t.ndim * (t.ndim + 1);
-    const size_t smem = (size_t)t.nC * P * sizeof(float);
+    const int block = 256;
+    const size_t smem = ((size_t)round4(t.nC * P) + block) * sizeof(float);
     Steps st;
     st.h = (float)(1.0 / nsteps);
     st.hh = (float)(0.5 / nsteps);
     st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
-    const int block = 256;
 #define CPAB_FIN(N, M)                                                                         \
     {                                                                                          \
         auto kern = k_finalize<N, M>;                                                          \

@@ -413,14 +413,16 @@ __device__ __forceinline__ void frechet_expm(const float (&Y0)[K][K], const floa
 }
 
 // Per-theta tail of the finalize kernels, run by one block after the summed
-// cell statistics are in g (shared memory, nC * N*(N+1) floats): map them to
+// cell statistics are in g (shared memory, nC * N*(N+1) floats; red is
+// blockDim.x floats of shared scratch): map them to
 // dL/dA (mode 0: G = h S (I + h/2 [A;0])^T + h^2/2 A_lin^T S; mode 1: adjoint
 // Frechet derivative of expm) and contract with the basis,
 // dtheta[k] = sum_i B[i, k] dA[i].
 template <int N, int MODE>
-__device__ __forceinline__ void finish_theta(float *g, const float *__restrict__ A_th, int nC,
-                                             const Steps &st, const float *__restrict__ basis,
-                                             int d, float *__restrict__ dth) {
+__device__ __forceinline__ void finish_theta(float *g, float *red, const float *__restrict__ A_th,
+                                             int nC, const Steps &st,
+                                             const float *__restrict__ basis, int d,
+                                             float *__restrict__ dth) {
     constexpr int P = N * (N + 1);
     const int tid = threadIdx.x, B = blockDim.x, G = nC * P;
     if constexpr (MODE == 0) {
@@ -473,10 +475,31 @@ __device__ __forceinline__ void finish_theta(float *g, const float *__restrict__
         }
         __syncthreads();
     }
-    for (int k = tid; k < d; k += B) {
+    if (d <= 0) return;
+    if (d > B) {
+        for (int k = tid; k < d; k += B) {
+            float acc = 0.f;
+            for (int i = 0; i < G; ++i) acc = fmaf(__ldg(basis + (long long)i * d + k), g[i], acc);
+            dth[k] = acc;
+        }
+        return;
+    }
+    // d <= B: `groups` threads per basis column each take every groups-th row;
+    // their partial sums are added in group order (red: B floats of shared
+    // memory)
+    const int groups = B / d;
+    const int k = tid % d, gi = tid / d;
+    if (gi < groups) {
         float acc = 0.f;
-        for (int i = 0; i < G; ++i) acc = fmaf(__ldg(basis + (long long)i * d + k), g[i], acc);
-        dth[k] = acc;
+        for (int i = gi; i < G; i += groups)
+            acc = fmaf(__ldg(basis + (long long)i * d + k), g[i], acc);
+        red[tid] = acc;
+    }
+    __syncthreads();
+    if (tid < d) {
+        float acc = 0.f;
+        for (int q = 0; q < groups; ++q) acc += red[q * d + tid];
+        dth[tid] = acc;
     }
 }
 

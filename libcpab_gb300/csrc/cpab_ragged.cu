@@ -344,7 +344,8 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
     if (dtheta)
-        finish_theta<1, MODE>(g, A + (long long)s * G, nC, st, basis, d, dtheta + (long long)s * d);
+        finish_theta<1, MODE>(g, g + round4(G), A + (long long)s * G, nC, st, basis, d,
+                              dtheta + (long long)s * d);
 }
 
 // ------------------------------- planning ------------------------------------
@@ -459,7 +460,7 @@ static cudaError_t launch_ra_t(const Tess &t, int nsteps, int block, int ppt, in
     kern<<<grid, block, smem, s>>>(t, nsteps, st, S, off, tile_off, ppt, a, ties, err);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     auto fin = k_ragged_finalize<MODE>;
-    const size_t fsmem = (size_t)t.nC * 2 * sizeof(float);
+    const size_t fsmem = ((size_t)round4(t.nC * 2) + 256) * sizeof(float);
     if (fsmem > 48 * 1024) {
         e = cudaFuncSetAttribute(fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);
         if (e != cudaSuccess) return e;
