@@ -55,7 +55,8 @@ def parse():
                     help='images per step (the headline workload uses 64; smaller values '
                          'are for profiling runs only)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
-    ap.add_argument('--leg', default='all', choices=['all', 'ragged', 'volume', 'interp'],
+    ap.add_argument('--leg', default='all',
+                    choices=['all', 'ragged', 'volume', 'interp', 'aligner'],
                     help='run only one of the side workloads and print its result (for '
                          'profiling runs)')
     ap.add_argument('--no-tune', action='store_true',
@@ -287,6 +288,7 @@ def run_gb300(args):
     ragged = run_ragged(device, args.steps, flush, tune=not args.no_tune) if extra else None
     volume = run_volume(device, args.steps, flush) if extra else None
     interp = run_interp_sweep(device, args.steps, flush) if extra else None
+    aligner = run_aligner(device) if extra else None
     clk = clocks.stop() if clocks else None
     status = N.device_status()
 
@@ -346,6 +348,7 @@ def run_gb300(args):
             'ragged_1d': ragged,
             'volume_3d': volume,
             'interpolate_2d': interp,
+            'aligner': aligner,
             'clocks': clk, 'device_status': status,
         }
     if world > 1:
@@ -525,6 +528,34 @@ def run_interp_sweep(device, steps, flush):
     return {'sweep': res, 'peak_gbs': peak, 'peak_source': src}
 
 
+def run_aligner(device, iters=100):
+    """CpabAligner.alignment_by_gradient on one 3 x 224 x 224 image (tess [3,3],
+    Adam, lr 1e-2): the eager loop (losses kept on the device) against the
+    same loop replayed from a CUDA graph."""
+    from libcpab_gb300 import Cpab, CpabAligner
+    T = Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True)
+    g = torch.Generator().manual_seed(4)
+    raw = torch.rand(1, CHANNELS, SIZE, SIZE, generator=g)
+    x1 = F.avg_pool2d(raw, 5, 1, 2, count_include_pad=False).to(device).contiguous()
+    th_true = (THETA_STD * torch.randn(1, T.get_theta_dim(), generator=g)).to(device)
+    with torch.no_grad():
+        x2 = T.transform_data(x1, th_true, [SIZE, SIZE])
+    A = CpabAligner(T)
+    res = {}
+    for name, graph in (('eager', False), ('graph', True)):
+        A.alignment_by_gradient(x1, x2, maxiter=5, graph=graph)     # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        A.alignment_by_gradient(x1, x2, maxiter=iters, graph=graph)
+        losses = A.losses.cpu()
+        dt = time.perf_counter() - t0
+        res[name] = {'iterations_per_s': iters / dt, 'final_loss': float(losses[-1]),
+                     'first_loss': float(losses[0])}
+    res['workload'] = ('alignment_by_gradient, 1 x 3 x 224^2, tess [3,3], %d Adam iterations '
+                       '(wall clock incl. graph capture)' % iters)
+    return res
+
+
 def cpu_reference_step(sample, orc, T_h, nc):
     """The reference's CPU implementation of one step on a sample of images:
     forward op + interpolation, interpolation backward, analytic-gradient
@@ -615,7 +646,8 @@ def main():
         flush = lambda: flush_buf.fill_(1.0)
         fn = {'ragged': lambda: run_ragged(device, args.steps, flush, tune=not args.no_tune),
               'volume': lambda: run_volume(device, args.steps, flush),
-              'interp': lambda: run_interp_sweep(device, args.steps, flush)}[args.leg]
+              'interp': lambda: run_interp_sweep(device, args.steps, flush),
+              'aligner': lambda: run_aligner(device)}[args.leg]
         print(json.dumps({'leg': args.leg, 'result': fn()}))
         return
     res = run_gb300(args)

@@ -202,6 +202,42 @@ CPAB_API int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, i
                                  unsigned long long *ties, void *stream);
 
 /*
+ * Composition T_K o ... o T_1 (1 <= K <= 4 transformations of the same ndim):
+ * the fused form of CpabSequential.transform_data (libcpab/sequential.py:
+ * 109-128), which there is one transform_grid call per transformation and an
+ * interpolation of the final grid.  nc holds K*ndim ints (stage k at
+ * nc + k*ndim), nsteps K ints, E a HOST array of K device pointers to each
+ * stage's compensated tables [nb, nC_k, ndim, ndim+1].  lin, outsize, data,
+ * out and grid_out (may be NULL; the final grid) as in cpab_transform_data.
+ */
+CPAB_API int cpab_sequential_transform_data(int ndim, int K, const int *nc, const int *nsteps,
+                                            const float *lin, const int *outsize,
+                                            const float *const *E, int nb, const float *data,
+                                            int C, const int *size, float *out, float *grid_out,
+                                            unsigned long long *ties, void *stream);
+
+/*
+ * Backward of cpab_sequential_transform_data with the reference's gradient
+ * semantics: its transform_grid gives the points no gradient
+ * (libcpab/pytorch/transformer.py:202), so of the thetas only the last
+ * transformation's gets one (dtheta_last [nb, d_last]); ddata as in
+ * cpab_transform_data_backward.  A_last, basis_last: the last stage's A tables
+ * and basis; grid_saved: the final grid (reference mode).  workspace:
+ * cpab_transform_data_backward_workspace() of the last stage.
+ */
+CPAB_API int cpab_sequential_transform_data_backward(int ndim, int K, const int *nc,
+                                                     const int *nsteps, int mode,
+                                                     const float *lin, const int *outsize,
+                                                     const float *const *E, const float *A_last,
+                                                     const float *grid_saved, int nb,
+                                                     const float *data, int C, const int *size,
+                                                     const float *basis_last, int d_last,
+                                                     const float *grad_out, float *ddata,
+                                                     float *dtheta_last, void *workspace,
+                                                     size_t workspace_bytes,
+                                                     unsigned long long *ties, void *stream);
+
+/*
  * Cell index of every point ([ndim, nP] -> int32 [nP]), bit-identical to the
  * reference's C++/CUDA lookup (libcpab/core/cpab_ops.cpp:26-190).
  */

@@ -5,6 +5,8 @@ Drop-in for the pytorch GPU path of libcpab: ``Cpab.transform_grid``,
 hand-written CUDA kernels behind the C ABI of include/cpab_gb300.h.
 """
 from .cpab import Cpab
+from .sequential import CpabSequential
+from .alignment import CpabAligner
 from . import functions
 
-__all__ = ['Cpab', 'functions']
+__all__ = ['Cpab', 'CpabSequential', 'CpabAligner', 'functions']

@@ -49,6 +49,10 @@ class TransformGrid(torch.autograd.Function):
         ctx.save_for_backward(points, A, E)
         ctx.params = params
         ctx.points_dim = points.dim()
+        ctx.theta_like = (theta_c.shape, theta_c.dtype, theta_c.device)
+        # no upstream gradient (e.g. the output only feeds the points of a
+        # later transformation) arrives as None instead of zeros
+        ctx.set_materialize_grads(False)
         return out
 
     @staticmethod
@@ -56,12 +60,20 @@ class TransformGrid(torch.autograd.Function):
     def backward(ctx, grad):
         points, A, E = ctx.saved_tensors
         params = ctx.params
-        if not (ctx.needs_input_grad[0] or ctx.needs_input_grad[1]):
+        if grad is None:
+            # the reference computes this gradient from a zero cotangent: zeros
+            shape, dtype, dev = ctx.theta_like
+            zeros = torch.zeros(shape, dtype=dtype, device=dev) if ctx.needs_input_grad[1] else None
+            return None, zeros, None
+        # the reference returns no gradient for the points
+        # (libcpab/pytorch/transformer.py:202); params.point_gradient opts in
+        want_p = ctx.needs_input_grad[0] and getattr(params, 'point_gradient', False)
+        if not (want_p or ctx.needs_input_grad[1]):
             return None, None, None
         dtheta, dpoints = N.backward(params.nc, params.nstepsolver, _mode(params), points, A, E,
                                      _basis(params, points.device),
                                      grad.to(torch.float32).contiguous(),
-                                     want_dpoints=ctx.needs_input_grad[0], ties=_ties(params))
+                                     want_dpoints=want_p, ties=_ties(params))
         if dpoints is not None and ctx.points_dim == 2:
             dpoints = dpoints.sum(dim=0)
         return dpoints, (dtheta if ctx.needs_input_grad[1] else None), None

@@ -48,6 +48,11 @@ _SIGS = {
                                      _i),
     'cpab_findcellidx': ([_i, _c_int_p, _vp, _ll, _vp, _vp, _vp], _i),
     'cpab_device_status': ([ctypes.POINTER(ctypes.c_uint), _i], _i),
+    'cpab_sequential_transform_data': ([_i, _i, _c_int_p, _c_int_p, _vp, _c_int_p, _vp, _i, _vp,
+                                        _i, _c_int_p, _vp, _vp, _vp, _vp], _i),
+    'cpab_sequential_transform_data_backward': ([_i, _i, _c_int_p, _c_int_p, _i, _vp, _c_int_p,
+                                                 _vp, _vp, _vp, _i, _vp, _i, _c_int_p, _vp, _i,
+                                                 _vp, _vp, _vp, _vp, _sz, _vp, _vp], _i),
     'cpab_ragged1d_workspace': ([_i, _i, _i], _sz),
     'cpab_ragged1d_forward': ([_i, _i, _vp, _i, _vp, _ll, _vp, _vp, _vp, _sz, _vp, _vp], _i),
     'cpab_ragged1d_backward': ([_i, _i, _i, _vp, _vp, _i, _vp, _ll, _vp, _i, _vp, _vp, _vp, _vp,
@@ -406,3 +411,69 @@ def ragged_tune(kind, nc, nsteps, mode, A, E, offsets, values, target, basis, lo
     ms = ctypes.c_float(0.0)
     _check(load().cpab_ragged1d_tune(int(kind), *args, shape, ctypes.byref(ms), _stream(dev)))
     return (shape[0], shape[1]), ms.value, res
+
+
+# ------------------------------- composition ------------------------------- #
+def _stage_args(ncs, nsteps, Es):
+    K = len(ncs)
+    ndim = len(ncs[0])
+    if any(len(n) != ndim for n in ncs):
+        raise ValueError('all transformations of a composition have the same dimension')
+    if len(nsteps) != K or len(Es) != K:
+        raise ValueError('one nsteps and one table per transformation')
+    for k, E in enumerate(Es):
+        _require(E, 'E[%d]' % k)
+    nc_flat = _ints([x for n in ncs for x in n])
+    ptrs = (ctypes.c_void_p * K)(*[E.data_ptr() for E in Es])
+    return K, ndim, nc_flat, _ints(nsteps), ptrs
+
+
+def sequential_transform_data(ncs, nsteps, lin, outsize, Es, data, save_grid=False, ties=None):
+    """Fused transform_data through T_K o ... o T_1 (ncs: K tessellations,
+    nsteps: K step counts, Es: K compensated tables)."""
+    K, ndim, ncf, nsf, ptrs = _stage_args(ncs, nsteps, Es)
+    _require(lin, 'lin')
+    _require(data, 'data')
+    nb, C = data.shape[0], data.shape[1]
+    nP = 1
+    for o in outsize:
+        nP *= int(o)
+    out = torch.empty((nb, C, *[int(o) for o in outsize]), device=data.device,
+                      dtype=torch.float32)
+    grid = torch.empty((nb, ndim, nP), device=data.device, dtype=torch.float32) \
+        if save_grid else None
+    _check(load().cpab_sequential_transform_data(ndim, K, ncf, nsf, _ptr(lin), _ints(outsize),
+                                                 ptrs, nb, _ptr(data), C, _ints(data.shape[2:]),
+                                                 _ptr(out), _ptr(grid), _ptr(ties),
+                                                 _stream(data.device)))
+    return out, grid
+
+
+def sequential_transform_data_backward(ncs, nsteps, mode, lin, outsize, Es, A_last, grid_saved,
+                                       data, basis_last, grad_out, want_ddata=True, ties=None,
+                                       workspace=None):
+    """(d(data), dtheta of the last transformation) of the fused composition."""
+    K, ndim, ncf, nsf, ptrs = _stage_args(ncs, nsteps, Es)
+    for t, name in ((lin, 'lin'), (A_last, 'A_last'), (data, 'data'), (basis_last, 'basis_last'),
+                    (grad_out, 'grad_out')):
+        _require(t, name)
+    if mode == GRAD_REFERENCE:
+        _require(grid_saved, 'grid_saved')
+    nb, C = data.shape[0], data.shape[1]
+    d = basis_last.shape[1]
+    dev = data.device
+    dtheta = torch.empty((nb, d), device=dev, dtype=torch.float32)
+    ddata = torch.empty_like(data) if want_ddata else None
+    lib = load()
+    need = lib.cpab_transform_data_backward_workspace(ndim, _ints(ncs[-1]), int(nsteps[-1]),
+                                                      int(mode), _ints(outsize), nb)
+    if need == 0 and nb > 0:
+        _check(3)
+    if workspace is None or workspace.numel() < need:
+        workspace = torch.empty(max(need, 1), device=dev, dtype=torch.uint8)
+    _check(lib.cpab_sequential_transform_data_backward(
+        ndim, K, ncf, nsf, int(mode), _ptr(lin), _ints(outsize), ptrs, _ptr(A_last),
+        _ptr(grid_saved), nb, _ptr(data), C, _ints(data.shape[2:]), _ptr(basis_last), d,
+        _ptr(grad_out), _ptr(ddata), _ptr(dtheta), _ptr(workspace), workspace.numel(),
+        _ptr(ties), _stream(dev)))
+    return ddata, dtheta

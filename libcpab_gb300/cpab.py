@@ -69,6 +69,7 @@ class Cpab(object):
         p.numeric_grad = False
         p.use_slow = False
         p.gradient = 'reference'
+        p.point_gradient = False
         if p.ndim == 1:
             p.nC = p.nc[0]
             p.params_pr_cell = 2
@@ -102,7 +103,7 @@ class Cpab(object):
         return self.params.basis
 
     def set_solver_params(self, nstepsolver=50, numeric_grad=False, use_slow=False,
-                          gradient=None):
+                          gradient=None, point_gradient=None):
         """Integration settings (libcpab/cpab.py:140-157).
 
         use_slow selected the reference's pure-PyTorch loop; the same
@@ -110,6 +111,10 @@ class Cpab(object):
         records the flag.  gradient ('reference' or 'exact') selects the
         backward: the reference's analytic (midpoint-rule sensitivity)
         gradient, or the exact derivative of the forward map.
+        point_gradient (default False, as the reference, whose
+        transform_grid returns no gradient for the points:
+        libcpab/pytorch/transformer.py:202) makes transform_grid also
+        return dL/dpoints, e.g. to train every stage of a composition.
         """
         assert nstepsolver > 0, 'nstepsolver must be a positive number'
         assert type(nstepsolver) == int, 'nstepsolver must be integer'
@@ -118,6 +123,9 @@ class Cpab(object):
         if gradient is not None:
             assert gradient in ('reference', 'exact'), "gradient must be 'reference' or 'exact'"
             self.params.gradient = gradient
+        if point_gradient is not None:
+            assert type(point_gradient) == bool, 'point_gradient must be bool'
+            self.params.point_gradient = point_gradient
         self.params.nstepsolver = nstepsolver
         self.params.numeric_grad = numeric_grad
         self.params.use_slow = use_slow

@@ -286,6 +286,26 @@ __device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nste
     warp_flush<P>(gcell >= 0 && live, gcell, acc, warp_tab);
 }
 
+// Sweep with the arithmetic of k_integrate's compensated path,
+// p <- p + E_c [p;1], nsteps times.  tabE may be in shared or global memory.
+template <int N>
+__device__ __forceinline__ void e_sweep(const float *tabE, const Tess &t, int nsteps,
+                                        float (&p)[N], unsigned long long *ties, unsigned *err) {
+    constexpr int P = N * (N + 1);
+    for (int s = 0; s < nsteps; ++s) {
+        int c = find_cell<N>(p, t, ties);
+        if ((unsigned)c >= (unsigned)t.nC) {
+            raise_error(err, kErrBadCell);
+            c = 0;
+        }
+        float M[P], y[N];
+        load_cell<N>(tabE, c, M);
+        affine_apply<N>(M, p, y);
+#pragma unroll
+        for (int r = 0; r < N; ++r) p[r] += y[r];
+    }
+}
+
 // Forward sweep that logs cells and checkpoints; p holds p_0 on entry and
 // p_N on exit.
 template <int N, int MODE, typename CT>

@@ -292,13 +292,16 @@ size_t cpab_transform_data_backward_workspace(int ndim, const int *nc, int nstep
     return plan.partial_floats * sizeof(float);
 }
 
-int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, int mode,
-                                 const float *lin, const int *outsize, const float *A,
-                                 const float *E, const float *grid_saved, int nb,
-                                 const float *data, int C, const int *size, const float *basis,
-                                 int d, const float *grad_out, float *ddata, float *dtheta,
-                                 void *workspace, size_t workspace_bytes,
-                                 unsigned long long *ties, void *stream) {
+}  // extern "C"
+
+// transform_data backward of the last transformation of a composition whose
+// earlier stages (pre, may be NULL) move the grid first.
+static int td_backward(int ndim, const int *nc, int nsteps, int mode, const float *lin,
+                       const int *outsize, const float *A, const float *E,
+                       const float *grid_saved, int nb, const float *data, int C,
+                       const int *size, const float *basis, int d, const float *grad_out,
+                       float *ddata, float *dtheta, void *workspace, size_t workspace_bytes,
+                       unsigned long long *ties, void *stream, const PreStages *pre) {
     g_err[0] = 0;
     Tess t;
     int rc = make_tess(ndim, nc, &t);
@@ -334,11 +337,90 @@ int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, int mode,
     float *partials = static_cast<float *>(workspace);
     cudaError_t e = launch_transform_data_backward(
         t, nsteps, mode, plan, lin, outsize, mode == CPAB_GRAD_EXACT ? E : A, grid_saved, nb, data,
-        C, size, grad_out, ddata, partials, ties, device_error_word(), s);
+        C, size, grad_out, ddata, partials, ties, device_error_word(), s, pre);
     if (e != cudaSuccess) return cuda_fail(e, "transform_data backward launch");
     if (d == 0) return CPAB_OK;
     e = launch_finalize(t, nsteps, mode, partials, plan.parts, A, basis, d, nb, dtheta, s);
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "finalize launch");
+}
+
+// Stages 0..K-1 of a composition (nc: K*ndim ints, nsteps: K ints, E: K
+// device pointers).
+static int make_stages(int ndim, int K, const int *nc, const int *nsteps,
+                       const float *const *E, SeqStages *sq) {
+    if (K < 1 || K > kMaxPre + 1)
+        return fail(CPAB_ERR_ARGUMENT, "a composition has 1 to %d transformations (got %d)",
+                    kMaxPre + 1, K);
+    if (!nc || !nsteps || !E) return fail(CPAB_ERR_ARGUMENT, "nc, nsteps or E is NULL");
+    sq->K = K;
+    for (int k = 0; k < K; ++k) {
+        int rc = make_tess(ndim, nc + k * ndim, &sq->t[k]);
+        if (rc) return rc;
+        if ((rc = check_steps(nsteps[k]))) return rc;
+        if (!E[k]) return fail(CPAB_ERR_ARGUMENT, "E[%d] is NULL", k);
+        sq->nsteps[k] = nsteps[k];
+        sq->E[k] = E[k];
+    }
+    return CPAB_OK;
+}
+
+extern "C" {
+
+int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, int mode,
+                                 const float *lin, const int *outsize, const float *A,
+                                 const float *E, const float *grid_saved, int nb,
+                                 const float *data, int C, const int *size, const float *basis,
+                                 int d, const float *grad_out, float *ddata, float *dtheta,
+                                 void *workspace, size_t workspace_bytes,
+                                 unsigned long long *ties, void *stream) {
+    return td_backward(ndim, nc, nsteps, mode, lin, outsize, A, E, grid_saved, nb, data, C, size,
+                       basis, d, grad_out, ddata, dtheta, workspace, workspace_bytes, ties,
+                       stream, nullptr);
+}
+
+int cpab_sequential_transform_data(int ndim, int K, const int *nc, const int *nsteps,
+                                   const float *lin, const int *outsize, const float *const *E,
+                                   int nb, const float *data, int C, const int *size, float *out,
+                                   float *grid_out, unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3");
+    SeqStages sq;
+    int rc = make_stages(ndim, K, nc, nsteps, E, &sq);
+    if (rc) return rc;
+    if ((rc = check_geo(ndim, size, outsize, nb))) return rc;
+    if (nb < 0 || C < 1) return fail(CPAB_ERR_ARGUMENT, "invalid nb or C");
+    if (nb == 0) return CPAB_OK;
+    if (!lin || !data || !out) return fail(CPAB_ERR_ARGUMENT, "lin, data or out is NULL");
+    cudaError_t e = launch_sequential_transform_data(sq, lin, outsize, nb, data, C, size, out,
+                                                     grid_out, ties, device_error_word(),
+                                                     as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "sequential transform_data launch");
+}
+
+int cpab_sequential_transform_data_backward(int ndim, int K, const int *nc, const int *nsteps,
+                                            int mode, const float *lin, const int *outsize,
+                                            const float *const *E, const float *A_last,
+                                            const float *grid_saved, int nb, const float *data,
+                                            int C, const int *size, const float *basis_last,
+                                            int d_last, const float *grad_out, float *ddata,
+                                            float *dtheta_last, void *workspace,
+                                            size_t workspace_bytes, unsigned long long *ties,
+                                            void *stream) {
+    g_err[0] = 0;
+    if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3");
+    SeqStages sq;
+    int rc = make_stages(ndim, K, nc, nsteps, E, &sq);
+    if (rc) return rc;
+    PreStages pre;
+    pre.K = K - 1;
+    for (int k = 0; k < K - 1; ++k) {
+        pre.t[k] = sq.t[k];
+        pre.nsteps[k] = sq.nsteps[k];
+        pre.E[k] = sq.E[k];
+    }
+    return td_backward(ndim, nc + (K - 1) * ndim, nsteps[K - 1], mode, lin, outsize, A_last,
+                       E[K - 1], grid_saved, nb, data, C, size, basis_last, d_last, grad_out,
+                       ddata, dtheta_last, workspace, workspace_bytes, ties, stream, &pre);
 }
 
 int cpab_findcellidx(int ndim, const int *nc, const float *points, long long nP, int *out,

@@ -130,8 +130,8 @@ cudaError_t launch_transform_data(const Tess &t, int nsteps, const float *lin, c
 
 template <int N, int MODE, typename CT>
 __global__ void __launch_bounds__(256)
-    k_transform_data_backward(Tess t, int nsteps, Steps st, Geo g, const float *__restrict__ lin,
-                              const float *__restrict__ table,
+    k_transform_data_backward(Tess t, int nsteps, Steps st, Geo g, PreStages pre,
+                              const float *__restrict__ lin, const float *__restrict__ table,
                               const float *__restrict__ grid_saved, int C,
                               const float *__restrict__ data, const float *__restrict__ gout,
                               float *__restrict__ ddata, float *__restrict__ partials, int parts,
@@ -154,6 +154,13 @@ __global__ void __launch_bounds__(256)
         else {
 #pragma unroll
             for (int r = 0; r < N; ++r) p[r] = 0.5f;
+        }
+        // composition: the transformations before this one move the grid first
+#pragma unroll
+        for (int k = 0; k < kMaxPre; ++k) {
+            if (k >= pre.K) break;
+            e_sweep<N>(pre.E[k] + (long long)b * pre.t[k].nC * (N * (N + 1)), pre.t[k],
+                       pre.nsteps[k], p, ties, err);
         }
         logged_forward<N, MODE, CT>(sm, t, nsteps, st, p, ties, err);
 #pragma unroll
@@ -232,7 +239,8 @@ bool plan_transform_data_backward(const Tess &t, int nsteps, int mode, long long
 
 template <int N, int MODE, typename CT>
 static cudaError_t launch_td_bwd_t(const Tess &t, int nsteps, const AdjointPlan &plan,
-                                   const Geo &g, const float *lin, const float *table,
+                                   const Geo &g, const PreStages &pre, const float *lin,
+                                   const float *table,
                                    const float *grid_saved, int nb, const float *data, int C,
                                    const float *gout, float *ddata, float *partials,
                                    unsigned long long *ties, unsigned *err, cudaStream_t s) {
@@ -247,7 +255,7 @@ static cudaError_t launch_td_bwd_t(const Tess &t, int nsteps, const AdjointPlan 
     if (nb == 0) return cudaSuccess;
     if (nb > 65535) return cudaErrorInvalidConfiguration;   // images on grid y
     const dim3 grid((unsigned)plan.parts, (unsigned)nb);
-    kern<<<grid, plan.block, plan.smem, s>>>(t, nsteps, st, g, lin, table, grid_saved, C,
+    kern<<<grid, plan.block, plan.smem, s>>>(t, nsteps, st, g, pre, lin, table, grid_saved, C,
                                                        data, gout, ddata, partials, plan.parts,
                                                        plan.tiles, ties, err);
     return cudaGetLastError();
@@ -260,21 +268,24 @@ cudaError_t launch_transform_data_backward(const Tess &t, int nsteps, int mode,
                                            int C, const int *size, const float *gout,
                                            float *ddata, float *partials,
                                            unsigned long long *ties, unsigned *err,
-                                           cudaStream_t s) {
+                                           cudaStream_t s, const PreStages *pre_in) {
     const Geo g = make_geo(t.ndim, size, outsize);
+    PreStages pre;
+    pre.K = 0;
+    if (pre_in) pre = *pre_in;
     const bool small = t.nC <= 256;
 #define CPAB_TDB(N)                                                                             \
     if (mode == 0)                                                                              \
-        return small ? launch_td_bwd_t<N, 0, uint8_t>(t, nsteps, plan, g, lin, table,           \
+        return small ? launch_td_bwd_t<N, 0, uint8_t>(t, nsteps, plan, g, pre, lin, table,           \
                                                       grid_saved, nb, data, C, gout, ddata,     \
                                                       partials, ties, err, s)                   \
-                     : launch_td_bwd_t<N, 0, uint16_t>(t, nsteps, plan, g, lin, table,          \
+                     : launch_td_bwd_t<N, 0, uint16_t>(t, nsteps, plan, g, pre, lin, table,          \
                                                        grid_saved, nb, data, C, gout, ddata,    \
                                                        partials, ties, err, s);                 \
-    return small ? launch_td_bwd_t<N, 1, uint8_t>(t, nsteps, plan, g, lin, table, grid_saved,   \
+    return small ? launch_td_bwd_t<N, 1, uint8_t>(t, nsteps, plan, g, pre, lin, table, grid_saved,   \
                                                   nb, data, C, gout, ddata, partials, ties,     \
                                                   err, s)                                       \
-                 : launch_td_bwd_t<N, 1, uint16_t>(t, nsteps, plan, g, lin, table, grid_saved,  \
+                 : launch_td_bwd_t<N, 1, uint16_t>(t, nsteps, plan, g, pre, lin, table, grid_saved,  \
                                                    nb, data, C, gout, ddata, partials, ties,    \
                                                    err, s);
     switch (t.ndim) {

@@ -75,6 +75,32 @@ cudaError_t launch_transform_data(const Tess &t, int nsteps, const float *lin, c
 bool plan_transform_data_backward(const Tess &t, int nsteps, int mode, long long nP, int nb,
                                   AdjointPlan *plan);
 
+// Transformations applied to the grid before the one being differentiated
+// (a composition T_K o ... o T_1 differentiated in theta_K only): their
+// compensated tables E_k [nb, nC_k, N, N+1] are read from global memory.
+constexpr int kMaxPre = 3;
+struct PreStages {
+    int K;
+    Tess t[kMaxPre];
+    int nsteps[kMaxPre];
+    const float *E[kMaxPre];
+};
+
+// Composition of up to kMaxPre + 1 transformations of one dimension: the grid
+// passes through all of them in one kernel, then data is sampled
+// (cpab_sequential.cu).  stages.E[k] are the compensated tables of stage k.
+struct SeqStages {
+    int K;
+    Tess t[kMaxPre + 1];
+    int nsteps[kMaxPre + 1];
+    const float *E[kMaxPre + 1];
+};
+cudaError_t launch_sequential_transform_data(const SeqStages &sq, const float *lin,
+                                             const int *outsize, int nb, const float *data,
+                                             int C, const int *size, float *out,
+                                             float *grid_out, unsigned long long *ties,
+                                             unsigned *err, cudaStream_t s);
+
 // Fused transform_data backward: given dL/dout, produce d(data) (accumulated)
 // and the partial cell gradients for launch_finalize.
 cudaError_t launch_transform_data_backward(const Tess &t, int nsteps, int mode,
@@ -84,7 +110,7 @@ cudaError_t launch_transform_data_backward(const Tess &t, int nsteps, int mode,
                                            int C, const int *size, const float *gout,
                                            float *ddata, float *partials,
                                            unsigned long long *ties, unsigned *err,
-                                           cudaStream_t s);
+                                           cudaStream_t s, const PreStages *pre = nullptr);
 
 // Ragged batched 1D series (cpab_ragged.cu).  Series s has the points
 // torch.linspace(0, 1, L_s) and the values values[off[s] .. off[s+1]).

@@ -109,25 +109,6 @@ __device__ __forceinline__ int find_series(const int *tile_off, int S, int t) {
     return lo;
 }
 
-// E sweep with the arithmetic of k_integrate's compensated path: p <- p + E_c [p;1], nsteps times.
-template <int N>
-__device__ __forceinline__ void e_sweep(const float *tabE, const Tess &t, int nsteps,
-                                        float (&p)[N], unsigned long long *ties, unsigned *err) {
-    constexpr int P = N * (N + 1);
-    for (int s = 0; s < nsteps; ++s) {
-        int c = find_cell<N>(p, t, ties);
-        if ((unsigned)c >= (unsigned)t.nC) {
-            raise_error(err, kErrBadCell);
-            c = 0;
-        }
-        float M[P], y[N];
-        load_cell<N>(tabE, c, M);
-        affine_apply<N>(M, p, y);
-#pragma unroll
-        for (int r = 0; r < N; ++r) p[r] += y[r];
-    }
-}
-
 __device__ __forceinline__ Geo series_geo(int L) {
     Geo g;
     g.size[0] = L;

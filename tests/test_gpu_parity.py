@@ -156,6 +156,7 @@ def test_gradient_exact_mode(name, cuda):
     from oracle.oracle import fp64_autograd
     g = load_golden(name)
     T = make_cpab(g, 'exact')
+    T.set_solver_params(nstepsolver=NSTEPS, gradient='exact', point_gradient=True)
     nc = [int(x) for x in g['nc']]
     th = torch.tensor(g['theta'], device=cuda, requires_grad=True)
     pts = torch.tensor(g['grid_b'], device=cuda, requires_grad=True)
@@ -169,6 +170,22 @@ def test_gradient_exact_mode(name, cuda):
     assert r <= 1e-4, 'exact-mode dtheta rel err %.3g' % r
     rp = rel_err(pts.grad.cpu().numpy(), dpts)
     assert rp <= 1e-4, 'exact-mode dpoints rel err %.3g' % rp
+
+
+def test_points_get_no_gradient_by_default(cuda):
+    """As the reference's analytic gradient (libcpab/pytorch/transformer.py:
+    202): transform_grid gives the points no gradient unless point_gradient
+    is set."""
+    g = load_golden('2d_3x3_zb')
+    T = make_cpab(g)
+    th = torch.tensor(g['theta'], device=cuda, requires_grad=True)
+    pts = torch.tensor(g['grid_b'], device=cuda, requires_grad=True)
+    T.transform_grid(pts, th).sum().backward()
+    assert pts.grad is None and th.grad is not None
+    T.set_solver_params(nstepsolver=NSTEPS, point_gradient=True)
+    pts2 = torch.tensor(g['grid_b'], device=cuda, requires_grad=True)
+    T.transform_grid(pts2, th).sum().backward()
+    assert pts2.grad is not None and torch.isfinite(pts2.grad).all()
 
 
 @pytest.mark.parametrize('name', SMALL)
