@@ -28,9 +28,8 @@ struct Corner {
 // Floor and clamp are done in float (NaN -> 0, huge -> edge, as a saturating
 // conversion does) and the small integers are read from the float bits.
 template <int N>
-__device__ __forceinline__ Corner<N> corners(const float (&p)[N], const Geo &g) {
-    Corner<N> cr;
-    int i0[N], i1[N];
+__device__ __forceinline__ void corner_indices(const float (&p)[N], const Geo &g, int (&i0)[N],
+                                               int (&i1)[N], float (&f)[N]) {
 #pragma unroll
     for (int j = 0; j < N; ++j) {
         const float x = p[j] * g.sizem1[j];
@@ -40,8 +39,15 @@ __device__ __forceinline__ Corner<N> corners(const float (&p)[N], const Geo &g) 
         const float b = fminf(fmaxf(fl + 1.f, 0.f), g.sizem1[j]);
         i0[j] = small_float_to_int(a);
         i1[j] = small_float_to_int(b);
-        cr.f[j] = x - a;
+        f[j] = x - a;
     }
+}
+
+template <int N>
+__device__ __forceinline__ Corner<N> corners(const float (&p)[N], const Geo &g) {
+    Corner<N> cr;
+    int i0[N], i1[N];
+    corner_indices<N>(p, g, i0, i1, cr.f);
 #pragma unroll
     for (int m = 0; m < (1 << N); ++m) {
         int o = 0;
@@ -53,20 +59,26 @@ __device__ __forceinline__ Corner<N> corners(const float (&p)[N], const Geo &g) 
 }
 
 // Lerp in the reference's order: along x first, then y, then z.
+// v[m]: corner values, corner bit j = axis j high.
 template <int N>
-__device__ __forceinline__ float lerp_corners(const float *D, const Corner<N> &cr) {
-    float v[1 << N];
-#pragma unroll
-    for (int m = 0; m < (1 << N); ++m) v[m] = __ldg(D + cr.off[m]);
+__device__ __forceinline__ float lerp_values(float (&v)[1 << N], const float (&f)[N]) {
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-        const float w1 = cr.f[j], w0 = 1.f - cr.f[j];
+        const float w1 = f[j], w0 = 1.f - f[j];
 #pragma unroll
         for (int m = 0; m < (1 << (N - 1 - j)); ++m)
             v[m] = __fadd_rn(__fmul_rn(v[2 * m], w0), __fmul_rn(v[2 * m + 1], w1));
         // after pass j, v[m] holds the lerp over axes 0..j for corner bits above j
     }
     return v[0];
+}
+
+template <int N>
+__device__ __forceinline__ float lerp_corners(const float *D, const Corner<N> &cr) {
+    float v[1 << N];
+#pragma unroll
+    for (int m = 0; m < (1 << N); ++m) v[m] = __ldg(D + cr.off[m]);
+    return lerp_values<N>(v, cr.f);
 }
 
 // Offsets in corner order for lerp_corners: pass j pairs entries (2m, 2m+1),
