@@ -14,8 +14,8 @@
 //     reference's arithmetic.
 // The result is bit-identical to the reference lookup for every float input.
 // The FP64 branch is taken only for genuine near-ties (a point within ~2e-6 of
-// a diagonal or plane), non-finite input, and 3D points outside the unit box
-// in x or y; it is counted when a counter is supplied.
+// a diagonal or plane, including 3D points pushed onto a domain corner) and
+// non-finite input; it is counted when a counter is supplied.
 //
 // Tables
 // ------
@@ -55,6 +55,7 @@ struct Tess {
     float wlim[3];    // (float)nc * inc     (float product)
     float clamp3[3];  // 3D clamp limits (float)(nc*inc - 1e-8), z uses inc_x
     int band[3];      // 1 if (float)(nc*inc) > nc*inc: floats in [nc*inc, wlim) exist
+    int band_any;     // band[0] | band[1] | band[2]
     float ncf[3];     // nc as float
 };
 
@@ -86,6 +87,7 @@ inline int tess_init(int ndim, const int *nc, Tess *t) {
         t->rinc[j] = (float)(1.0 / (double)t->inc[j]);
         t->wlim[j] = (float)n * t->inc[j];
         t->band[j] = (double)t->wlim[j] > (double)n * (double)t->inc[j];
+        t->band_any |= t->band[j];
         t->ncf[j] = (float)n;
         cells *= n;
     }
@@ -243,16 +245,20 @@ CPAB_HD inline int cell_2d_fast(float px, float py, const Tess &t) {
     const float ci = fminf(fmaxf(fi, 0.f), t.ncf[0] - 1.f);
     const float cj = fminf(fmaxf(fj, 0.f), t.ncf[1] - 1.f);
     // In-domain points past nc*inc (possible only when the float product
-    // nc*inc rounds above it) get the fmod remainder, not the continuous one.
-    if ((t.band[0] && fi > ci && px < t.wlim[0]) || (t.band[1] && fj > cj && py < t.wlim[1]))
+    // nc*inc rounds above it: band_any, fixed per tessellation) get the fmod
+    // remainder, not the continuous one.
+    if (t.band_any &&
+        ((t.band[0] && fi > ci && px < t.wlim[0]) || (t.band[1] && fj > cj && py < t.wlim[1])))
         return -1;
     const float x = fmaf(ri, t.rinc[0], fi - ci);
     const float y = fmaf(rj, t.rinc[1], fj - cj);
     const float dxy = x - y, sxy = (x + y) - 1.f;
     const float m = kMargin2 * ((1.f + fabsf(x)) + fabsf(y));
     if (!(fabsf(dxy) > m) || !(fabsf(sxy) > m)) return -1;
-    const float tri = dxy < 0.f ? (sxy > 0.f ? 2.f : 3.f) : (sxy > 0.f ? 1.f : 0.f);
-    return small_float_to_int(fmaf(4.f, fmaf(cj, t.ncf[0], ci), tri));
+    // triangle: 0 (dxy >= 0, sxy <= 0), 1 (dxy >= 0, sxy > 0), 2 (dxy < 0,
+    // sxy > 0), 3 (dxy < 0, sxy <= 0) = (sxy > 0) xor (dxy < 0 ? 3 : 0)
+    const int tri = (sxy > 0.f ? 1 : 0) ^ (dxy < 0.f ? 3 : 0);
+    return small_float_to_int(4.f * fmaf(cj, t.ncf[0], ci)) + tri;
 }
 
 __device__ __forceinline__ int cell_2d(float px, float py, const Tess &t,
