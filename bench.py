@@ -56,7 +56,7 @@ def parse():
                          'are for profiling runs only)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--leg', default='all',
-                    choices=['all', 'ragged', 'volume', 'interp', 'aligner'],
+                    choices=['all', 'ragged', 'volume', 'interp', 'aligner', 'exact'],
                     help='run only one of the side workloads and print its result (for '
                          'profiling runs)')
     ap.add_argument('--no-tune', action='store_true',
@@ -289,6 +289,7 @@ def run_gb300(args):
     volume = run_volume(device, args.steps, flush) if extra else None
     interp = run_interp_sweep(device, args.steps, flush) if extra else None
     aligner = run_aligner(device) if extra else None
+    exact = run_exact_flow(device, args.steps, flush) if extra else None
     clk = clocks.stop() if clocks else None
     status = N.device_status()
 
@@ -349,6 +350,7 @@ def run_gb300(args):
             'volume_3d': volume,
             'interpolate_2d': interp,
             'aligner': aligner,
+            'exact_flow': exact,
             'clocks': clk, 'device_status': status,
         }
     if world > 1:
@@ -556,6 +558,35 @@ def run_aligner(device, iters=100):
     return res
 
 
+def run_exact_flow(device, steps, flush):
+    """The opt-in exact-flow scheme on the headline grid (tess [3,3],
+    64 theta ~ N(0, 0.25 I), 224^2 grid): transform_grid forward, against the
+    fixed-step scheme on the same points."""
+    from libcpab_gb300 import Cpab, _native as N
+    from libcpab_gb300.functions import basis_on
+    T = Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True)
+    theta = (THETA_STD * torch.randn(BATCH, T.get_theta_dim(),
+                                     generator=torch.Generator().manual_seed(0))).to(device)
+    basis = basis_on(T.params, device)
+    A, _, E = N.cell_tables(NC, NSTEPS, theta, basis)
+    grid = T.uniform_meshgrid([SIZE, SIZE])
+    for _ in range(3):
+        N.integrate_exact(NC, grid, A)
+        N.integrate(NC, NSTEPS, grid, E)
+    t_ex = time_events(lambda: N.integrate_exact(NC, grid, A), steps, flush)
+    t_fs = time_events(lambda: N.integrate(NC, NSTEPS, grid, E), steps, flush)
+    cnt = torch.zeros(1, dtype=torch.int64, device=device)
+    ex = N.integrate_exact(NC, grid, A, steps=cnt)
+    fs = N.integrate(NC, NSTEPS, grid, E)
+    pts = BATCH * SIZE * SIZE
+    ms_ex, ms_fs = sum(t_ex) / len(t_ex), sum(t_fs) / len(t_fs)
+    return {'workload': 'transform_grid, tess [3,3] zero_boundary, 64 theta ~ N(0,0.25I), '
+                        '224^2 grid',
+            'exact_ms': ms_ex, 'exact_points_per_s': pts / (ms_ex / 1e3),
+            'fixed_step_ms': ms_fs, 'in_cell_steps_per_point': int(cnt.item()) / pts,
+            'max_abs_diff_exact_vs_fixed_step': float((ex - fs).abs().max())}
+
+
 def cpu_reference_step(sample, orc, T_h, nc):
     """The reference's CPU implementation of one step on a sample of images:
     forward op + interpolation, interpolation backward, analytic-gradient
@@ -647,7 +678,8 @@ def main():
         fn = {'ragged': lambda: run_ragged(device, args.steps, flush, tune=not args.no_tune),
               'volume': lambda: run_volume(device, args.steps, flush),
               'interp': lambda: run_interp_sweep(device, args.steps, flush),
-              'aligner': lambda: run_aligner(device)}[args.leg]
+              'aligner': lambda: run_aligner(device),
+              'exact': lambda: run_exact_flow(device, args.steps, flush)}[args.leg]
         print(json.dumps({'leg': args.leg, 'result': fn()}))
         return
     res = run_gb300(args)

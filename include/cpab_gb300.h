@@ -53,6 +53,7 @@ extern "C" {
 #define CPAB_DEV_BAD_CELL 2u    /* a cell index fell outside [0, nC)             */
 #define CPAB_DEV_SCRATCH 4u     /* a kernel's scratch region was too small       */
 #define CPAB_DEV_BAD_OFFSETS 8u /* a ragged series had invalid offsets (skipped) */
+#define CPAB_DEV_ITER_LIMIT 16u /* an exact-flow trajectory hit its step limit     */
 
 /* Message of the calling thread's last error ("" if none). */
 CPAB_API const char *cpab_last_error(void);
@@ -200,6 +201,20 @@ CPAB_API int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, i
                                  int d, const float *grad_out, float *ddata, float *dtheta,
                                  void *workspace, size_t workspace_bytes,
                                  unsigned long long *ties, void *stream);
+
+/*
+ * Exact-flow scheme (opt-in; no counterpart in the reference, whose
+ * integrator is the fixed-step scheme of cpab_forward / cpab_integrate,
+ * libcpab/core/cpab_ops.cu:268-388): each point follows the true flow of the
+ * continuous piecewise-affine field for time 1.  A: velocity tables
+ * [n_theta, nC, ndim, ndim+1] (cpab_cell_tables).  1D in closed form, 2D/3D
+ * by certified in-cell steps of the analytic cell flow.  steps (device
+ * uint64, may be NULL) accumulates the in-cell steps taken.  Forward only.
+ */
+CPAB_API int cpab_integrate_exact(int ndim, const int *nc, const float *points, int broadcast,
+                                  long long nP, const float *A, int n_theta, float *out,
+                                  unsigned long long *ties, unsigned long long *steps,
+                                  void *stream);
 
 /*
  * Composition T_K o ... o T_1 (1 <= K <= 4 transformations of the same ndim):

@@ -44,8 +44,13 @@ class TransformGrid(torch.autograd.Function):
         points = points.detach().to(torch.float32).contiguous()
         theta_c = theta.detach().to(torch.float32).contiguous()
         basis = _basis(params, theta.device)
-        A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis)
-        out = N.integrate(params.nc, params.nstepsolver, points, E, ties=_ties(params))
+        ctx.exact = getattr(params, 'integration', 'fixed_step') == 'exact'
+        if ctx.exact:
+            A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis, want_E=False)
+            out = N.integrate_exact(params.nc, points, A, ties=_ties(params))
+        else:
+            A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis)
+            out = N.integrate(params.nc, params.nstepsolver, points, E, ties=_ties(params))
         ctx.save_for_backward(points, A, E)
         ctx.params = params
         ctx.points_dim = points.dim()
@@ -60,6 +65,9 @@ class TransformGrid(torch.autograd.Function):
     def backward(ctx, grad):
         points, A, E = ctx.saved_tensors
         params = ctx.params
+        if ctx.exact:
+            raise NotImplementedError("the 'exact' integration scheme is forward only; use "
+                                      "integration='fixed_step' for gradients")
         if grad is None:
             # the reference computes this gradient from a zero cotangent: zeros
             shape, dtype, dev = ctx.theta_like

@@ -32,6 +32,7 @@ _SIGS = {
     'cpab_forward': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _vp], _i),
     'cpab_integrate': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _vp, _vp], _i),
     'cpab_integrate_trace': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _vp, _vp], _i),
+    'cpab_integrate_exact': ([_i, _c_int_p, _vp, _i, _ll, _vp, _i, _vp, _vp, _vp, _vp], _i),
     'cpab_backward_workspace': ([_i, _c_int_p, _i, _ll, _i], _sz),
     'cpab_backward': ([_i, _c_int_p, _i, _i, _vp, _i, _ll, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp,
                        _vp, _sz, _vp, _vp], _i),
@@ -174,6 +175,21 @@ def integrate(nc, nsteps, points, E, ties=None):
     out = torch.empty((n_theta, ndim, nP), device=points.device, dtype=torch.float32)
     _check(load().cpab_integrate(ndim, _ints(nc), int(nsteps), _ptr(points), broadcast, nP,
                                  _ptr(E), n_theta, _ptr(out), _ptr(ties), _stream(points.device)))
+    return out
+
+
+def integrate_exact(nc, points, A, ties=None, steps=None):
+    """Exact flow of the field A for time 1 (opt-in scheme, forward only)."""
+    _require(points, 'points')
+    _require(A, 'A')
+    ndim = len(nc)
+    n_theta = A.shape[0]
+    broadcast = int(points.dim() == 3 and points.shape[0] == n_theta)
+    nP = points.shape[-1]
+    out = torch.empty((n_theta, ndim, nP), device=points.device, dtype=torch.float32)
+    _check(load().cpab_integrate_exact(ndim, _ints(nc), _ptr(points), broadcast, nP, _ptr(A),
+                                       n_theta, _ptr(out), _ptr(ties), _ptr(steps),
+                                       _stream(points.device)))
     return out
 
 

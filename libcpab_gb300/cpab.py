@@ -70,6 +70,7 @@ class Cpab(object):
         p.use_slow = False
         p.gradient = 'reference'
         p.point_gradient = False
+        p.integration = 'fixed_step'
         if p.ndim == 1:
             p.nC = p.nc[0]
             p.params_pr_cell = 2
@@ -103,7 +104,7 @@ class Cpab(object):
         return self.params.basis
 
     def set_solver_params(self, nstepsolver=50, numeric_grad=False, use_slow=False,
-                          gradient=None, point_gradient=None):
+                          gradient=None, point_gradient=None, integration=None):
         """Integration settings (libcpab/cpab.py:140-157).
 
         use_slow selected the reference's pure-PyTorch loop; the same
@@ -115,6 +116,10 @@ class Cpab(object):
         transform_grid returns no gradient for the points:
         libcpab/pytorch/transformer.py:202) makes transform_grid also
         return dL/dpoints, e.g. to train every stage of a composition.
+        integration: 'fixed_step' (default, the reference's scheme: nstepsolver
+        steps of the cell's step map, the cell chosen at the start of each
+        step) or 'exact' (opt-in: the true flow of the continuous field for
+        time 1, with cell crossings; forward only, nstepsolver unused).
         """
         assert nstepsolver > 0, 'nstepsolver must be a positive number'
         assert type(nstepsolver) == int, 'nstepsolver must be integer'
@@ -123,6 +128,10 @@ class Cpab(object):
         if gradient is not None:
             assert gradient in ('reference', 'exact'), "gradient must be 'reference' or 'exact'"
             self.params.gradient = gradient
+        if integration is not None:
+            assert integration in ('fixed_step', 'exact'), \
+                "integration must be 'fixed_step' or 'exact'"
+            self.params.integration = integration
         if point_gradient is not None:
             assert type(point_gradient) == bool, 'point_gradient must be bool'
             self.params.point_gradient = point_gradient

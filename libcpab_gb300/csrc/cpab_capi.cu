@@ -156,6 +156,22 @@ int cpab_integrate(int ndim, const int *nc, int nsteps, const float *points, int
                             nullptr, ties, stream);
 }
 
+int cpab_integrate_exact(int ndim, const int *nc, const float *points, int broadcast,
+                         long long nP, const float *A, int n_theta, float *out,
+                         unsigned long long *ties, unsigned long long *steps, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if (nP < 0 || n_theta < 0) return fail(CPAB_ERR_ARGUMENT, "negative size");
+    if ((rc = check_theta_count(n_theta))) return rc;
+    if (nP == 0 || n_theta == 0) return CPAB_OK;
+    if (!points || !A || !out) return fail(CPAB_ERR_ARGUMENT, "points, A or out is NULL");
+    cudaError_t e = launch_integrate_exact(t, points, broadcast ? 1 : 0, nP, A, n_theta, out, ties,
+                                           device_error_word(), steps, as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "exact-flow launch");
+}
+
 int cpab_integrate_trace(int ndim, const int *nc, int nsteps, const float *points, int broadcast,
                          long long nP, const float *E, int n_theta, float *out, int *cells,
                          void *stream) {

@@ -41,6 +41,7 @@ enum : unsigned {
     kErrBadCell = 1u << 1,      // a cell index fell outside [0, nC)
     kErrScratch = 1u << 2,      // a kernel's scratch region was too small
     kErrBadOffsets = 1u << 3,   // a ragged series had invalid offsets (skipped)
+    kErrIterLimit = 1u << 4,    // an exact-flow trajectory hit its step limit
 };
 
 // Host-computed description of one tessellation.  The float constants are

@@ -112,6 +112,14 @@ cudaError_t launch_transform_data_backward(const Tess &t, int nsteps, int mode,
                                            unsigned long long *ties, unsigned *err,
                                            cudaStream_t s, const PreStages *pre = nullptr);
 
+// Exact-flow integration (cpab_exact.cu): the true flow of the continuous
+// piecewise-affine field for time 1 (table A: velocity maps).  steps
+// (nullable) accumulates the number of in-cell steps taken.
+cudaError_t launch_integrate_exact(const Tess &t, const float *points, int broadcast,
+                                   long long nP, const float *A, int n_theta, float *out,
+                                   unsigned long long *ties, unsigned *err,
+                                   unsigned long long *steps, cudaStream_t s);
+
 // Ragged batched 1D series (cpab_ragged.cu).  Series s has the points
 // torch.linspace(0, 1, L_s) and the values values[off[s] .. off[s+1]).
 constexpr long long kRaggedMaxLen = 1ll << 22;   // per-series length limit

@@ -13,86 +13,9 @@
 // I + (small) and so keeps the increment E to full FP32 relative precision.
 // The integrator then advances p <- p + E [p;1]; with T stored directly the
 // per-step increment would carry an absolute error of ~1 ulp of 1.
-#include "cpab_launch.h"
+#include "cpab_expm.cuh"
 
 namespace cpab {
-
-template <int N>
-__device__ __forceinline__ void matmul_nn(const float (&a)[N][N], const float (&b)[N][N],
-                                          float (&c)[N][N]) {
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int j = 0; j < N; ++j) {
-            float acc = 0.f;
-#pragma unroll
-            for (int k = 0; k < N; ++k) acc = fmaf(a[i][k], b[k][j], acc);
-            c[i][j] = acc;
-        }
-}
-
-// E = expm([[M, v],[0,0]]) - I restricted to the top N rows, for M = dt*A_lin,
-// v = dt*A_trans.  Outputs E_lin (N x N) and E_t (N).
-template <int N>
-__device__ __forceinline__ void expm1_affine(const float (&M)[N][N], const float (&v)[N],
-                                             float (&El)[N][N], float (&Et)[N]) {
-    float norm = 0.f;
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-        float s = 0.f;
-#pragma unroll
-        for (int i = 0; i < N; ++i) s += fabsf(M[i][j]);
-        norm = fmaxf(norm, s);
-    }
-    int sq = 0;
-    if (norm > 0.5f) sq = min(64, (int)ceilf(log2f(norm / 0.5f)));
-    const float scale = ldexpf(1.f, -sq);
-    float Y[N][N];
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int j = 0; j < N; ++j) Y[i][j] = M[i][j] * scale;
-    // Horner: phi(Y) = I + Y/2 (I + Y/3 (I + ... (I + Y/11)))
-    float P[N][N];
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int j = 0; j < N; ++j) P[i][j] = (i == j) ? 1.f : 0.f;
-    for (int k = 11; k >= 2; --k) {
-        float YP[N][N];
-        matmul_nn<N>(Y, P, YP);
-        const float r = 1.f / (float)k;
-#pragma unroll
-        for (int i = 0; i < N; ++i)
-#pragma unroll
-            for (int j = 0; j < N; ++j) P[i][j] = fmaf(YP[i][j], r, (i == j) ? 1.f : 0.f);
-    }
-    // phi(2Y) = phi(Y) (I + Y phi(Y)/2), repeated sq times.
-    for (int s = 0; s < sq; ++s) {
-        float YP[N][N], W[N][N], Pn[N][N];
-        matmul_nn<N>(Y, P, YP);
-#pragma unroll
-        for (int i = 0; i < N; ++i)
-#pragma unroll
-            for (int j = 0; j < N; ++j) W[i][j] = fmaf(YP[i][j], 0.5f, (i == j) ? 1.f : 0.f);
-        matmul_nn<N>(P, W, Pn);
-#pragma unroll
-        for (int i = 0; i < N; ++i)
-#pragma unroll
-            for (int j = 0; j < N; ++j) {
-                P[i][j] = Pn[i][j];
-                Y[i][j] *= 2.f;
-            }
-    }
-    matmul_nn<N>(M, P, El);
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-        float acc = 0.f;
-#pragma unroll
-        for (int k = 0; k < N; ++k) acc = fmaf(P[i][k], v[k], acc);
-        Et[i] = acc;
-    }
-}
 
 template <int N>
 __global__ void __launch_bounds__(128)

@@ -177,7 +177,7 @@ def transform_data(data, theta, params, outsize):
     if data.shape[0] != theta.shape[0]:
         raise ValueError('data and theta must have the same batch size (%d vs %d)'
                          % (data.shape[0], theta.shape[0]))
-    if params.numeric_grad:
+    if params.numeric_grad or getattr(params, 'integration', 'fixed_step') == 'exact':
         grid = uniform_meshgrid(params.ndim, params.domain_min, params.domain_max, outsize,
                                 data.device)
         return interpolate(params.ndim, data, transformer(grid, theta, params), outsize)

@@ -152,7 +152,9 @@ class CpabSequential(object):
         plist = [c.params for c in self.cpab]
         fused = (1 <= self.n_cpab <= 4
                  and not any(getattr(p, 'point_gradient', False) for p in plist)
-                 and not any(p.numeric_grad for p in plist))
+                 and not any(p.numeric_grad for p in plist)
+                 and all(getattr(p, 'integration', 'fixed_step') == 'fixed_step'
+                         for p in plist))
         if not fused:
             grid = self.uniform_meshgrid(outsize)
             grid_t = self.transform_grid(grid, thetas)

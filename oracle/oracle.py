@@ -444,3 +444,39 @@ def fp64_autograd(basis, theta, points, nc, cotangent, nsteps=50, cells=None):
     w = torch.as_tensor(np.asarray(cotangent, dtype=np.float64))
     (out * w).sum().backward()
     return out.detach().numpy(), th.grad.numpy(), pts.grad.numpy()
+
+
+# --------------------------------------------------------------------------- #
+# FP64 oracle of the exact-flow scheme
+# --------------------------------------------------------------------------- #
+def exact_flow_fp64(basis, theta, points, nc, rtol=1e-12, atol=1e-13):
+    """Flow of the continuous piecewise-affine field for time 1, in float64.
+
+    An independent check of the exact-flow kernels: instead of their
+    in-cell analytic steps, the ODE dx/dt = v(x) is integrated for all points
+    of one theta at once by scipy's DOP853 with tight tolerances.  v uses the
+    C++ cell rules (numpy_findcellidx, semantics='cpp'); the field is
+    continuous across faces, so which side a point on a face is given to does
+    not matter.  Returns [n_theta, ndim, nP]."""
+    from scipy.integrate import solve_ivp
+    nc = list(nc)
+    ndim = len(nc)
+    B = np.asarray(basis, dtype=np.float64)
+    th = np.asarray(theta, dtype=np.float64)
+    nC = B.shape[0] // (ndim * (ndim + 1))
+    pts = np.asarray(points, dtype=np.float64)
+    nP = pts.shape[-1]
+    out = np.empty((th.shape[0], ndim, nP))
+    for k in range(th.shape[0]):
+        A = (B @ th[k]).reshape(nC, ndim, ndim + 1)
+        p0 = pts[k] if pts.ndim == 3 else pts
+
+        def field(_t, y):
+            P = y.reshape(ndim, nP)
+            c = numpy_findcellidx(ndim, P.astype(np.float32), nc, semantics='cpp')
+            Ph = np.concatenate([P, np.ones((1, nP))], axis=0)
+            return np.einsum('nij,jn->in', A[c], Ph).reshape(-1)
+        sol = solve_ivp(field, (0.0, 1.0), p0.reshape(-1), method='DOP853', rtol=rtol,
+                        atol=atol)
+        out[k] = sol.y[:, -1].reshape(ndim, nP)
+    return out

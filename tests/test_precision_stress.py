@@ -196,6 +196,38 @@ def other_configs(cuda, orc):
     return rep
 
 
+def exact_flow_errors(cuda):
+    """Opt-in exact-flow scheme vs its FP64 oracle (ODE integration), per
+    workload distribution, on 4 theta x 1000 random points."""
+    from libcpab_gb300 import _native as N
+    from libcpab_gb300.tessellation import make_tessellation
+    from conftest import load_golden
+    from oracle.oracle import exact_flow_fp64
+    rep = {}
+    for name, nc, zb, vp, std in (('cfg1 1D [50] zb', [50], True, False, 1.0),
+                                  ('cfg2 2D [3,3] zb', [3, 3], True, False, 0.5),
+                                  ('cfg3 1D [100] free', [100], False, False, 1.0),
+                                  ('cfg4 3D [4,4,4] zb vp', [4, 4, 4], True, True, 1.0),
+                                  ('cfg5 2D [8,8] free, N(0,9I)', [8, 8], False, False, 3.0)):
+        B = load_golden('L_3d_4x4x4_zb_vp')['B'] if nc == [4, 4, 4] else \
+            make_tessellation(nc, zb, vp).B
+        rng = np.random.default_rng(7)
+        theta = (std * rng.standard_normal((4, B.shape[1]))).astype(np.float32)
+        pts = rng.random((len(nc), 1000)).astype(np.float32)
+        basis = torch.tensor(np.ascontiguousarray(B), dtype=torch.float32, device=cuda)
+        A, _, _ = N.cell_tables(nc, 50, torch.tensor(theta, device=cuda), basis, want_E=False)
+        steps = torch.zeros(1, dtype=torch.int64, device=cuda)
+        out = N.integrate_exact(nc, torch.tensor(pts, device=cuda), A, steps=steps).cpu().numpy()
+        ref = exact_flow_fp64(B, theta, pts, nc)
+        err = np.abs(out - ref).max(axis=1)
+        scale = np.maximum(1.0, np.abs(ref).max(axis=1))
+        rep[name] = {'max_err': float(err.max()), 'max_err_scaled': float((err / scale).max()),
+                     'p99_err': float(np.quantile(err, 0.99)),
+                     'in_cell_steps_per_point': int(steps.item()) / err.size,
+                     'device_status': N.device_status()}
+    return rep
+
+
 def main():
     from libcpab_gb300.tessellation import make_tessellation
     from oracle.oracle import Oracle
@@ -210,6 +242,7 @@ def main():
     report['large'] = evaluate(theta[:32], pts, cuda, orc)
     report['near_identity'] = evaluate(theta[256:288], pts, cuda, orc)
     report['other_configs'] = other_configs(cuda, orc)
+    report['exact_flow'] = exact_flow_errors(cuda)
     # GPU-only: FP64 tie lookups over the whole configuration
     from libcpab_gb300 import _native as N
     B = make_tessellation(NC, False, False).B
