@@ -110,9 +110,6 @@ __device__ __forceinline__ void adjoint_step(const float *dtab, int c, const flo
     for (int k = 0; k < N; ++k) lam[k] = nl[k];
 }
 
-template <typename CT>
-__host__ __device__ constexpr int cell_bytes() { return (int)sizeof(CT); }
-
 __host__ __device__ inline int round4(int x) { return (x + 3) & ~3; }
 
 // Shared memory carve-up for the adjoint kernels (floats unless noted):

@@ -39,7 +39,6 @@ constexpr int kMaxDim = 3;
 enum : unsigned {
     kErrTmaTimeout = 1u << 0,   // a bulk copy into shared memory did not complete
     kErrBadCell = 1u << 1,      // a cell index fell outside [0, nC)
-    kErrScratch = 1u << 2,      // a kernel's scratch region was too small
     kErrBadOffsets = 1u << 3,   // a ragged series had invalid offsets (skipped)
     kErrIterLimit = 1u << 4,    // an exact-flow trajectory hit its step limit
 };

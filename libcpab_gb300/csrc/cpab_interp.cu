@@ -27,13 +27,15 @@ namespace cpab {
 
 constexpr unsigned kMaxGridY = 65535;
 
+// 1D: grid order is output order.
 template <int N>
 __global__ void __launch_bounds__(256)
     k_interpolate(Geo g, const float *__restrict__ data, int C, const float *__restrict__ grid,
                   float *__restrict__ out, int nb) {
+    static_assert(N == 1, "2D and 3D use k_interpolate_tiled");
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= g.nP) return;
-    const int oo = out_offset<N>(k, g);
+    const int oo = k;
     for (int b = blockIdx.y; b < nb; b += gridDim.y) {
         float p[N];
 #pragma unroll
@@ -51,9 +53,10 @@ __global__ void __launch_bounds__(256)
     k_interpolate_backward(Geo g, const float *__restrict__ data, int C,
                            const float *__restrict__ grid, const float *__restrict__ gout,
                            float *__restrict__ ddata, float *__restrict__ dgrid, int nb) {
+    static_assert(N == 1, "2D and 3D use k_interpolate_backward_tiled");
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= g.nP) return;
-    const int oo = out_offset<N>(k, g);
+    const int oo = k;
     for (int b = blockIdx.y; b < nb; b += gridDim.y) {
         float p[N];
 #pragma unroll

@@ -87,24 +87,6 @@ __device__ __forceinline__ float lerp_corners(const float *D, const Corner<N> &c
 // with m^1 (axis 0), leaving entries indexed by the remaining bits (axis 1 as
 // bit 0), and so on.
 
-// Output element offset of point k within one (b, c) plane: [W_out(, H_out(, D_out))]
-// with the last axis fastest, while k has axis 0 fastest.
-template <int N>
-__device__ __forceinline__ int out_offset(int k, const Geo &g) {
-    if constexpr (N == 1) return k;
-    else if constexpr (N == 2) {
-        const unsigned iy = fast_div((unsigned)k, g.dout[0]);
-        const unsigned ix = (unsigned)k - iy * g.outsize[0];
-        return (int)(ix * g.outsize[1] + iy);
-    } else {
-        const unsigned r = fast_div((unsigned)k, g.dout[0]);
-        const unsigned ix = (unsigned)k - r * g.outsize[0];
-        const unsigned iz = fast_div(r, g.dout[1]);
-        const unsigned iy = r - iz * g.outsize[1];
-        return (int)((ix * g.outsize[1] + iy) * g.outsize[2] + iz);
-    }
-}
-
 // d(lerp)/d(f_j) and the per-corner weights, for the backward passes.
 template <int N>
 __device__ __forceinline__ void lerp_grads(const float *D, const Corner<N> &cr, float w,
