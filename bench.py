@@ -56,7 +56,7 @@ def parse():
                          'are for profiling runs only)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--leg', default='all',
-                    choices=['all', 'ragged', 'volume', 'interp', 'aligner', 'exact'],
+                    choices=['all', 'ragged', 'volume', 'interp', 'aligner', 'exact', 'points'],
                     help='run only one of the side workloads and print its result (for '
                          'profiling runs)')
     ap.add_argument('--no-tune', action='store_true',
@@ -290,6 +290,7 @@ def run_gb300(args):
     interp = run_interp_sweep(device, args.steps, flush) if extra else None
     aligner = run_aligner(device) if extra else None
     exact = run_exact_flow(device, args.steps, flush) if extra else None
+    points = run_ragged_points(device, args.steps, flush) if extra else None
     clk = clocks.stop() if clocks else None
     status = N.device_status()
 
@@ -351,6 +352,7 @@ def run_gb300(args):
             'interpolate_2d': interp,
             'aligner': aligner,
             'exact_flow': exact,
+            'ragged_points_2d': points,
             'clocks': clk, 'device_status': status,
         }
     if world > 1:
@@ -434,6 +436,72 @@ def run_ragged(device, steps, flush, tune=True):
             'tuned_shape_forward': list(shape_f) if shape_f else None,
             'forward_only_ms': ms_f,
             'loss': loss}
+
+
+POINTS_S, POINTS_LEN = 1024, (256, 16384)
+
+
+def run_ragged_points(device, steps, flush):
+    """Ragged point sets in 2D (tess [3,3] zero_boundary, the headline
+    tessellation): 1,024 sets of U{256..16384} points ~ U[0,1]^2, theta ~
+    N(0, 0.25 I) per set.  Forward alone and forward + dtheta backward
+    (reference gradient) in one persistent launch each, on the points as given
+    and on the points sorted by starting cell; beside them the padded
+    alternative (one batched transform_grid call on sets padded to the
+    longest)."""
+    from libcpab_gb300 import Cpab, _native as N
+    from libcpab_gb300.functions import basis_on, findcellidx
+    T = Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True)
+    g = torch.Generator().manual_seed(3)
+    theta = (THETA_STD * torch.randn(POINTS_S, T.get_theta_dim(), generator=g)).to(device)
+    lengths = torch.randint(POINTS_LEN[0], POINTS_LEN[1] + 1, (POINTS_S,), generator=g)
+    off = torch.cat([torch.zeros(1, dtype=torch.int64), torch.cumsum(lengths, 0)]).to(device)
+    total = int(lengths.sum())
+    pts = torch.rand(2, total, generator=g).to(device)
+    basis = basis_on(T.params, device)
+    A, _, E = N.cell_tables(NC, NSTEPS, theta, basis)
+    gout = torch.randn(2, total, generator=g).to(device)
+    nC = N.num_cells(NC)
+    pos = torch.arange(total, device=device)
+    sid = torch.searchsorted(off, pos, right=True) - 1
+    perm = torch.sort(sid * nC + findcellidx(2, pts, NC), stable=True).indices
+    pts_sorted, gout_sorted = pts[:, perm].contiguous(), gout[:, perm].contiguous()
+    wsf = N.ragged_points_workspace(NC, POINTS_S, device)
+    wsb = N.ragged_points_workspace(NC, POINTS_S, device)
+    res = {}
+    for tag, P, G in (('unsorted', pts, gout), ('sorted', pts_sorted, gout_sorted)):
+        fwd = lambda: N.ragged_points_forward(NC, NSTEPS, E, off, P, workspace=wsf)
+        bwd = lambda: N.ragged_points_backward(NC, NSTEPS, 0, A, E, off, P, basis, G,
+                                               workspace=wsb)
+        for _ in range(3):
+            fwd(); bwd()
+        tf = time_events(fwd, steps, flush)
+        tb = time_events(bwd, steps, flush)
+        ms_f, ms_b = sum(tf) / len(tf), sum(tb) / len(tb)
+        res[tag] = {'forward_ms': ms_f, 'backward_ms': ms_b,
+                    'forward_points_per_s': total / (ms_f / 1e3),
+                    'fwd_bwd_points_per_s': total / ((ms_f + ms_b) / 1e3)}
+    # the padded alternative: sets padded to the longest, one batched call
+    Lmax = int(lengths.max())
+    padded = torch.full((POINTS_S, 2, Lmax), 0.5, device=device)
+    for s in range(POINTS_S):
+        a, b = int(off[s]), int(off[s + 1])
+        padded[s, :, :b - a] = pts[:, a:b]
+    gpad = torch.zeros_like(padded)
+    for _ in range(2):
+        N.integrate(NC, NSTEPS, padded, E)
+    tp = time_events(lambda: N.integrate(NC, NSTEPS, padded, E), max(2, steps // 4), flush)
+    tpb = time_events(lambda: N.backward(NC, NSTEPS, 0, padded, A, E, basis, gpad),
+                      max(2, steps // 4), flush)
+    ms_p, ms_pb = sum(tp) / len(tp), sum(tpb) / len(tpb)
+    res['padded_batch'] = {'forward_ms': ms_p, 'backward_ms': ms_pb,
+                           'fwd_bwd_points_per_s': total / ((ms_p + ms_pb) / 1e3),
+                           'padded_points': POINTS_S * Lmax}
+    res['workload'] = ('ragged point sets 2D: %d sets of U{%d..%d} points ~ U[0,1]^2 (total %d), '
+                       'tess [3,3] zero_boundary, theta ~ N(0,0.25I) per set; forward and '
+                       'forward+dtheta (reference gradient), one persistent launch each'
+                       % (POINTS_S, POINTS_LEN[0], POINTS_LEN[1], total))
+    return res
 
 
 def hbm_peak():
@@ -679,7 +747,8 @@ def main():
               'volume': lambda: run_volume(device, args.steps, flush),
               'interp': lambda: run_interp_sweep(device, args.steps, flush),
               'aligner': lambda: run_aligner(device),
-              'exact': lambda: run_exact_flow(device, args.steps, flush)}[args.leg]
+              'exact': lambda: run_exact_flow(device, args.steps, flush),
+              'points': lambda: run_ragged_points(device, args.steps, flush)}[args.leg]
         print(json.dumps({'leg': args.leg, 'result': fn()}))
         return
     res = run_gb300(args)

@@ -332,6 +332,50 @@ CPAB_API int cpab_ragged1d_tune(int kind, int nc, int nsteps, int mode, const fl
                                 size_t workspace_bytes, int *shape, float *best_ms, void *stream);
 
 /*
+ * Ragged point sets: S sets of ndim-dimensional points, each moved by its
+ * own theta, in one persistent launch.  Replaces one transform_grid call per
+ * (theta, point set) pair (libcpab/cpab.py:276-302 ->
+ * libcpab/pytorch/transformer.py:72-87, the cpab_gpu.forward /
+ * cpab_gpu.backward pair of libcpab/pytorch/transformer_cuda.cpp:17-70), or
+ * one call on sets padded to a common size.  No counterpart in the reference.
+ *
+ * points is [ndim, total] (coordinate-major like cpab_integrate's points);
+ * set s owns the columns offsets[s] .. offsets[s+1] (L_s points,
+ * 0 <= L_s < 2^22); offsets is a DEVICE array of S + 1 int64 (a set with
+ * invalid offsets is skipped and raises CPAB_DEV_BAD_OFFSETS).
+ * total + 128*S must be below 2^31.  A and E are [S, nC, ndim, ndim+1] (one
+ * theta per set, from cpab_cell_tables); basis is [nC*ndim*(ndim+1), d];
+ * dtheta is [S, d].  Each set's result equals cpab_integrate / cpab_backward
+ * on that set alone (same arithmetic, same lookups; dtheta up to the order of
+ * the float sums).  workspace is device memory of
+ * cpab_ragged_points_workspace() bytes; the calls do not synchronise and can
+ * be captured in a CUDA graph.  Warps are most efficient when nearby points
+ * of a set start in the same cell (e.g. points sorted by starting cell).
+ */
+CPAB_API size_t cpab_ragged_points_workspace(int ndim, const int *nc, int S);
+
+/* out [ndim, total]: set s's points integrated with its table E[s]. */
+CPAB_API int cpab_ragged_points_forward(int ndim, const int *nc, int nsteps, const float *E,
+                                        int S, const long long *offsets, long long total,
+                                        const float *points, float *out, void *workspace,
+                                        size_t workspace_bytes, unsigned long long *ties,
+                                        void *stream);
+
+/*
+ * Backward of cpab_ragged_points_forward from grad_out = dL/d(out)
+ * [ndim, total]: dtheta [S, d] (overwritten; deterministic) and dpoints
+ * [ndim, total] (overwritten, may be NULL).  Mode as in cpab_backward
+ * (CPAB_GRAD_REFERENCE needs A; CPAB_GRAD_EXACT needs A and E).
+ */
+CPAB_API int cpab_ragged_points_backward(int ndim, const int *nc, int nsteps, int mode,
+                                         const float *A, const float *E, int S,
+                                         const long long *offsets, long long total,
+                                         const float *basis, int d, const float *points,
+                                         const float *grad_out, float *dtheta, float *dpoints,
+                                         void *workspace, size_t workspace_bytes,
+                                         unsigned long long *ties, void *stream);
+
+/*
  * Synchronise the current device and report the device error word (the
  * CPAB_DEV_* bits raised by kernels since the last clear).  clear != 0 resets
  * it.  Returns CPAB_OK, or CPAB_ERR_CUDA if the device reported an error.

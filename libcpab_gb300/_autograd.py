@@ -7,6 +7,8 @@ Interpolate    -- interpolation with its backward (libcpab/pytorch/interpolation
 TransformData  -- fused meshgrid -> integrate -> sample (libcpab/cpab.py:304-331)
 TransformDataRagged -- the same for many 1D series of uneven lengths in one
                   persistent launch (one theta per series)
+TransformGridRagged -- transformer for many point sets of uneven sizes, one
+                  theta per set, in one persistent launch
 
 Gradient modes (params.gradient):
   'reference' -- the reference's analytic gradient: the midpoint-rule
@@ -203,3 +205,35 @@ class TransformDataRagged(torch.autograd.Function):
             _basis(params, values.device), grad.to(torch.float32).contiguous(),
             want_dvalues=want_v, ties=_ties(params))
         return dvalues, (dtheta if want_t else None), None, None
+
+
+class TransformGridRagged(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, points, theta, offsets, params):
+        points_c = points.detach().to(torch.float32).contiguous()
+        theta_c = theta.detach().to(torch.float32).contiguous()
+        basis = _basis(params, points.device)
+        mode = _mode(params)
+        A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis)
+        out = N.ragged_points_forward(params.nc, params.nstepsolver, E, offsets, points_c,
+                                      ties=_ties(params))
+        ctx.save_for_backward(points_c, offsets, A, E if mode == N.GRAD_EXACT else None)
+        ctx.params = params
+        ctx.mode = mode
+        return out
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, grad):
+        points, offsets, A, E = ctx.saved_tensors
+        params = ctx.params
+        # as in TransformGrid: no point gradient unless params.point_gradient
+        want_p = ctx.needs_input_grad[0] and getattr(params, 'point_gradient', False)
+        want_t = ctx.needs_input_grad[1]
+        if not (want_p or want_t):
+            return None, None, None, None
+        dtheta, dpoints = N.ragged_points_backward(
+            params.nc, params.nstepsolver, ctx.mode, A, E, offsets, points,
+            _basis(params, points.device), grad.to(torch.float32).contiguous(),
+            want_dpoints=want_p, ties=_ties(params))
+        return dpoints, (dtheta if want_t else None), None, None

@@ -63,6 +63,11 @@ _SIGS = {
     'cpab_ragged1d_tune': ([_i, _i, _i, _i, _vp, _vp, _i, _vp, _ll, _vp, _i, _vp, _vp,
                             ctypes.c_float, _vp, _vp, _vp, _vp, _vp, _sz, _c_int_p,
                             ctypes.POINTER(ctypes.c_float), _vp], _i),
+    'cpab_ragged_points_workspace': ([_i, _c_int_p, _i], _sz),
+    'cpab_ragged_points_forward': ([_i, _c_int_p, _i, _vp, _i, _vp, _ll, _vp, _vp, _vp, _sz, _vp,
+                                    _vp], _i),
+    'cpab_ragged_points_backward': ([_i, _c_int_p, _i, _i, _vp, _vp, _i, _vp, _ll, _vp, _i, _vp,
+                                     _vp, _vp, _vp, _vp, _sz, _vp, _vp], _i),
 }
 
 EXPORTED = tuple(_SIGS)
@@ -493,3 +498,58 @@ def sequential_transform_data_backward(ncs, nsteps, mode, lin, outsize, Es, A_la
         _ptr(grad_out), _ptr(ddata), _ptr(dtheta), _ptr(workspace), workspace.numel(),
         _ptr(ties), _stream(dev)))
     return ddata, dtheta
+
+
+# --------------------------- ragged point sets ------------------------------ #
+def _points_common(nc, offsets, points):
+    _require(offsets, 'offsets', torch.int64)
+    _require(points, 'points')
+    if offsets.dim() != 1 or offsets.numel() < 1:
+        raise ValueError('offsets must be a 1D tensor of S + 1 entries')
+    if points.dim() != 2 or points.shape[0] != len(nc):
+        raise ValueError('points must be [ndim, total] with ndim = %d' % len(nc))
+    return len(nc), offsets.numel() - 1, points.shape[1]
+
+
+def ragged_points_workspace(nc, S, device, workspace=None):
+    need = load().cpab_ragged_points_workspace(len(nc), _ints(nc), int(S))
+    if need == 0 and S > 0:
+        _check(1)
+    if workspace is None or workspace.numel() < need:
+        workspace = torch.empty(max(need, 1), device=device, dtype=torch.uint8)
+    return workspace
+
+
+def ragged_points_forward(nc, nsteps, E, offsets, points, ties=None, workspace=None):
+    """Each set's points integrated with its own table: out [ndim, total]."""
+    ndim, S, total = _points_common(nc, offsets, points)
+    _require(E, 'E')
+    dev = points.device
+    out = torch.empty_like(points)
+    ws = ragged_points_workspace(nc, S, dev, workspace)
+    _check(load().cpab_ragged_points_forward(ndim, _ints(nc), int(nsteps), _ptr(E), S,
+                                             _ptr(offsets), total, _ptr(points), _ptr(out),
+                                             _ptr(ws), ws.numel(), _ptr(ties), _stream(dev)))
+    return out
+
+
+def ragged_points_backward(nc, nsteps, mode, A, E, offsets, points, basis, grad_out,
+                           want_dpoints=False, ties=None, workspace=None):
+    """(dtheta [S, d], dpoints [ndim, total] or None) from dL/d(out)."""
+    ndim, S, total = _points_common(nc, offsets, points)
+    _require(A, 'A')
+    _require(basis, 'basis')
+    _require(grad_out, 'grad_out')
+    if E is not None:
+        _require(E, 'E')
+    dev = points.device
+    d = basis.shape[1]
+    dtheta = torch.empty((S, d), device=dev, dtype=torch.float32)
+    dpoints = torch.empty_like(points) if want_dpoints else None
+    ws = ragged_points_workspace(nc, S, dev, workspace)
+    _check(load().cpab_ragged_points_backward(ndim, _ints(nc), int(nsteps), int(mode), _ptr(A),
+                                              _ptr(E), S, _ptr(offsets), total, _ptr(basis), d,
+                                              _ptr(points), _ptr(grad_out), _ptr(dtheta),
+                                              _ptr(dpoints), _ptr(ws), ws.numel(), _ptr(ties),
+                                              _stream(dev)))
+    return dtheta, dpoints

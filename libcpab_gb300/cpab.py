@@ -224,6 +224,16 @@ class Cpab(object):
         self._check_type(theta); self._check_device(theta)
         return self.backend.transform_data_ragged(values, offsets, theta, self.params)
 
+    def transform_grid_ragged(self, points, offsets, theta, sort_by_cell=False):
+        """Ragged batch of point sets (extension; no reference counterpart):
+        set s = points[:, offsets[s]:offsets[s+1]] moved by theta[s] as
+        transform_grid(points_s, theta[s:s+1]) would, all in one launch.
+        points [ndim, total] float32, offsets [S+1] int64 (CUDA)."""
+        self._check_type(points); self._check_device(points)
+        self._check_type(theta); self._check_device(theta)
+        return self.backend.transform_grid_ragged(points, offsets, theta, self.params,
+                                                  sort_by_cell=sort_by_cell)
+
     def ragged_mse(self, values, target, offsets, theta, **kwargs):
         """Fused forward + mean-squared-error loss + backward for ragged 1D
         series (extension).  Returns a dict with loss, sse, dtheta, dvalues."""

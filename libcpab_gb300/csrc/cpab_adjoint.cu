@@ -148,10 +148,7 @@ static cudaError_t launch_adjoint_t(const Tess &t, int nsteps, const AdjointPlan
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)plan.smem);
     if (e != cudaSuccess) return e;
-    Steps st;
-    st.h = (float)(1.0 / nsteps);
-    st.hh = (float)(0.5 / nsteps);
-    st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
+    const Steps st = make_steps(nsteps);
     if (n_theta == 0) return cudaSuccess;
     if (n_theta > 65535) return cudaErrorInvalidConfiguration;   // theta on grid y
     const dim3 grid((unsigned)plan.parts, (unsigned)n_theta);
@@ -225,10 +222,7 @@ cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *pa
     const int P = t.ndim * (t.ndim + 1);
     const int block = 256;
     const size_t smem = ((size_t)round4(t.nC * P) + block) * sizeof(float);
-    Steps st;
-    st.h = (float)(1.0 / nsteps);
-    st.hh = (float)(0.5 / nsteps);
-    st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
+    const Steps st = make_steps(nsteps);
 #define CPAB_FIN(N, M)                                                                         \
     {                                                                                          \
         auto kern = k_finalize<N, M>;                                                          \

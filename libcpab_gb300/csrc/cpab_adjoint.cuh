@@ -12,6 +12,14 @@ struct Steps {
     float h, hh, hh2;   // 1/N, 1/(2N), 1/(2N^2)
 };
 
+inline Steps make_steps(int nsteps) {
+    Steps st;
+    st.h = (float)(1.0 / nsteps);
+    st.hh = (float)(0.5 / nsteps);
+    st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
+    return st;
+}
+
 // One forward step of the trajectory that the adjoint differentiates.
 template <int N, int MODE>
 __device__ __forceinline__ void traj_step(const float *tab, int c, const Steps &st,

@@ -708,6 +708,85 @@ int cpab_ragged1d_tune(int kind, int nc, int nsteps, int mode, const float *A, c
     return run(bb, bp);   // leave the outputs of the chosen shape
 }
 
+// ---------------------------- ragged point sets ------------------------------
+size_t cpab_ragged_points_workspace(int ndim, const int *nc, int S) {
+    g_err[0] = 0;
+    Tess t;
+    if (make_tess(ndim, nc, &t)) return 0;
+    if (S < 0) {
+        fail(CPAB_ERR_ARGUMENT, "need S >= 0");
+        return 0;
+    }
+    return ragged_points_workspace_bytes(t, S);
+}
+
+static int check_ragged_points(int ndim, const int *nc, int nsteps, int S, long long total,
+                               const long long *offsets, void *workspace,
+                               size_t workspace_bytes, Tess *t) {
+    int rc = make_tess(ndim, nc, t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if (S < 0 || total < 0) return fail(CPAB_ERR_ARGUMENT, "need S >= 0 and total >= 0");
+    if (total + (long long)S * 128 >= (1ll << 31))
+        return fail(CPAB_ERR_UNSUPPORTED, "total + 128 * S must be below 2^31");
+    if (S == 0) return CPAB_OK;
+    if (!offsets) return fail(CPAB_ERR_ARGUMENT, "offsets is NULL");
+    const size_t need = ragged_points_workspace_bytes(*t, S);
+    if (!workspace || workspace_bytes < need)
+        return fail(CPAB_ERR_WORKSPACE, "workspace of %zu bytes needed (got %zu)", need,
+                    workspace ? workspace_bytes : (size_t)0);
+    return CPAB_OK;
+}
+
+int cpab_ragged_points_forward(int ndim, const int *nc, int nsteps, const float *E, int S,
+                               const long long *offsets, long long total, const float *points,
+                               float *out, void *workspace, size_t workspace_bytes,
+                               unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = check_ragged_points(ndim, nc, nsteps, S, total, offsets, workspace,
+                                 workspace_bytes, &t);
+    if (rc) return rc;
+    if (S == 0 || total == 0) return CPAB_OK;
+    if (!E || !points || !out) return fail(CPAB_ERR_ARGUMENT, "E, points or out is NULL");
+    cudaError_t e = launch_ragged_points_forward(t, nsteps, S, offsets, total, E, points, out,
+                                                 workspace, ties, device_error_word(),
+                                                 as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "ragged points forward launch");
+}
+
+int cpab_ragged_points_backward(int ndim, const int *nc, int nsteps, int mode, const float *A,
+                                const float *E, int S, const long long *offsets,
+                                long long total, const float *basis, int d,
+                                const float *points, const float *grad_out, float *dtheta,
+                                float *dpoints, void *workspace, size_t workspace_bytes,
+                                unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = check_ragged_points(ndim, nc, nsteps, S, total, offsets, workspace,
+                                 workspace_bytes, &t);
+    if (rc) return rc;
+    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+        return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
+    if (d < 0) return fail(CPAB_ERR_ARGUMENT, "negative d");
+    if (S == 0) return CPAB_OK;
+    if (!A || (mode == CPAB_GRAD_EXACT && !E) || (total > 0 && (!points || !grad_out)) ||
+        (d > 0 && (!basis || !dtheta)))
+        return fail(CPAB_ERR_ARGUMENT, "A, E, points, grad_out, basis or dtheta is NULL");
+    cudaStream_t s = as_stream(stream);
+    if (dpoints && total > 0) {
+        cudaError_t e = cudaMemsetAsync(dpoints, 0, (size_t)total * ndim * sizeof(float), s);
+        if (e != cudaSuccess) return cuda_fail(e, "memset");
+    }
+    cudaError_t e = launch_ragged_points_backward(t, nsteps, mode, S, offsets, total, A, E,
+                                                  points, grad_out, dpoints, basis, d,
+                                                  d > 0 ? dtheta : nullptr, workspace, ties,
+                                                  device_error_word(), s);
+    if (e == cudaErrorInvalidConfiguration)
+        return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "ragged points adjoint launch");
+}
+
 }  // extern "C"
 
 // --------------------------------------------------------------------------

@@ -248,10 +248,7 @@ static cudaError_t launch_td_bwd_t(const Tess &t, int nsteps, const AdjointPlan 
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)plan.smem);
     if (e != cudaSuccess) return e;
-    Steps st;
-    st.h = (float)(1.0 / nsteps);
-    st.hh = (float)(0.5 / nsteps);
-    st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
+    const Steps st = make_steps(nsteps);
     if (nb == 0) return cudaSuccess;
     if (nb > 65535) return cudaErrorInvalidConfiguration;   // images on grid y
     const dim3 grid((unsigned)plan.parts, (unsigned)nb);

@@ -156,6 +156,22 @@ cudaError_t launch_ragged_adjoint(const Tess &t, int nsteps, int mode, bool fuse
                                   float *sse, void *ws, unsigned long long *ties, unsigned *err,
                                   cudaStream_t s);
 
+// Ragged point sets of any dimension (cpab_ragged_points.cu): set s owns the
+// columns offsets[s] .. offsets[s+1] of points [ndim, total] and has its own
+// cell tables (E, A: [S, nC, ndim, ndim+1]).
+size_t ragged_points_workspace_bytes(const Tess &t, int S);
+cudaError_t launch_ragged_points_forward(const Tess &t, int nsteps, int S, const long long *off,
+                                         long long total, const float *E, const float *points,
+                                         float *out, void *ws, unsigned long long *ties,
+                                         unsigned *err, cudaStream_t s);
+cudaError_t launch_ragged_points_backward(const Tess &t, int nsteps, int mode, int S,
+                                          const long long *off, long long total, const float *A,
+                                          const float *E, const float *points,
+                                          const float *gout, float *dpoints, const float *basis,
+                                          int d, float *dtheta, void *ws,
+                                          unsigned long long *ties, unsigned *err,
+                                          cudaStream_t s);
+
 int num_sms();
 
 }  // namespace cpab

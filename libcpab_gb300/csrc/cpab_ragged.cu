@@ -35,7 +35,7 @@
 #include <mutex>
 #include <tuple>
 
-#include "cpab_adjoint.cuh"
+#include "cpab_ragged.cuh"
 #include "cpab_interp.cuh"
 
 namespace cpab {
@@ -46,10 +46,6 @@ namespace cpab {
 __device__ __forceinline__ float linspace01(int j, int L, float step) {
     if (L == 1) return 0.f;
     return (j < (L >> 1)) ? __fmul_rn(step, (float)j) : fmaf(-step, (float)(L - 1 - j), 1.f);
-}
-
-__device__ __forceinline__ bool series_ok(long long a, long long b, long long total) {
-    return a >= 0 && b >= a && b <= total && b - a < kRaggedMaxLen;
 }
 
 // Warp-tile prefix over series (one block): tile_off[s] = sum_{s'<s} tiles(s'),
@@ -98,15 +94,10 @@ __global__ void __launch_bounds__(1024)
     if (tid == B - 1) tile_off[S] = (int)run;
 }
 
-// Largest s with tile_off[s] <= t (tile_off[0] = 0 <= t < tile_off[S]).
-__device__ __forceinline__ int find_series(const int *tile_off, int S, int t) {
-    int lo = 0, hi = S;
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (__ldg(tile_off + mid) <= t) lo = mid;
-        else hi = mid;
-    }
-    return lo;
+cudaError_t launch_ragged_plan(int S, const long long *off, long long total, int tpw,
+                               int *tile_off, unsigned *err, cudaStream_t s) {
+    k_ragged_plan<<<1, 1024, 0, s>>>(S, off, total, tpw, tile_off, err);
+    return cudaGetLastError();
 }
 
 __device__ __forceinline__ Geo series_geo(int L) {
@@ -296,52 +287,12 @@ __global__ void __launch_bounds__(256)
     finish(s);
 }
 
-// ------------------------------- finalize ------------------------------------
-// One block per series: sum the series' partial slots in warp order, then the
-// per-theta tail shared with k_finalize.
-template <int MODE>
-__global__ void __launch_bounds__(256)
-    k_ragged_finalize(int nC, Steps st, int S, const int *__restrict__ tile_off, int TW,
-                      const float *__restrict__ partials, const float *__restrict__ sse_partials,
-                      const float *__restrict__ A, const float *__restrict__ basis, int d,
-                      float *__restrict__ dtheta, float *__restrict__ sse) {
-    extern __shared__ float4 smem4[];
-    float *g = reinterpret_cast<float *>(smem4);
-    const int s = blockIdx.x, tid = threadIdx.x, B = blockDim.x;
-    const int G = nC * 2;
-    const int TT = __ldg(tile_off + S);
-    const int K = max(1, (TT + TW - 1) / TW);
-    const int a = __ldg(tile_off + s), b = __ldg(tile_off + s + 1);
-    const int w0 = a / K, w1 = (b > a) ? (b - 1) / K : w0 - 1;
-    for (int i = tid; i < G; i += B) {
-        float acc = 0.f;
-        for (int w = w0; w <= w1; ++w) acc += __ldg(partials + ((long long)w + s) * G + i);
-        g[i] = acc;
-    }
-    if (sse && tid == 0) {
-        float acc = 0.f;
-        for (int w = w0; w <= w1; ++w) acc += __ldg(sse_partials + (long long)w + s);
-        sse[s] = acc;
-    }
-    __syncthreads();
-    if (dtheta)
-        finish_theta<1, MODE>(g, g + round4(G), A + (long long)s * G, nC, st, basis, d,
-                              dtheta + (long long)s * d);
-}
-
 // ------------------------------- planning ------------------------------------
 namespace {
 std::mutex g_tune_mu;
 // (device, kind, mode, nC, nsteps, S, total) -> (block, ppt)
 std::map<std::tuple<int, int, int, int, int, int, long long>, std::pair<int, int>> g_tuned;
 
-Steps make_steps(int nsteps) {
-    Steps st;
-    st.h = (float)(1.0 / nsteps);
-    st.hh = (float)(0.5 / nsteps);
-    st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
-    return st;
-}
 }  // namespace
 
 size_t ragged_workspace_bytes(const Tess &t, int S) {
@@ -440,7 +391,7 @@ static cudaError_t launch_ra_t(const Tess &t, int nsteps, int block, int ppt, in
     const Steps st = make_steps(nsteps);
     kern<<<grid, block, smem, s>>>(t, nsteps, st, S, off, tile_off, ppt, a, ties, err);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    auto fin = k_ragged_finalize<MODE>;
+    auto fin = k_ragged_finalize<1, MODE>;
     const size_t fsmem = ((size_t)round4(t.nC * 2) + 256) * sizeof(float);
     if (fsmem > 48 * 1024) {
         e = cudaFuncSetAttribute(fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem);

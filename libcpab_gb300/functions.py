@@ -226,6 +226,43 @@ def ragged_mse(values, target, offsets, theta, params, loss_scale=None, want_out
     return res
 
 
+def _check_ragged_points(points, offsets, theta, params):
+    if points.dim() != 2 or points.shape[0] != params.ndim:
+        raise ValueError('points must be [ndim=%d, total]' % params.ndim)
+    if offsets.dim() != 1 or offsets.dtype != torch.int64:
+        raise ValueError('offsets must be a 1D int64 tensor of n_sets + 1 entries')
+    if theta.dim() != 2 or theta.shape[0] != offsets.numel() - 1:
+        raise ValueError('theta must be [n_sets=%d, d]' % (offsets.numel() - 1))
+
+
+def transform_grid_ragged(points, offsets, theta, params, sort_by_cell=False):
+    """Ragged batch of point sets: set s is points[:, offsets[s]:offsets[s+1]]
+    and is moved by theta[s] exactly as transformer(points_s, theta[s:s+1],
+    params) would (libcpab/pytorch/transformer.py:72-87), all sets in one
+    launch.  points [ndim, total] float32, offsets [S+1] int64, theta [S, d];
+    returns [ndim, total].
+
+    sort_by_cell=True runs each set's points in the order of their starting
+    cell (a stable sort, undone on the output): the same result, faster when
+    a set's points are scattered over many cells."""
+    _require_cuda(points, offsets, theta)
+    _check_ragged_points(points, offsets, theta, params)
+    from ._autograd import TransformGridRagged
+    offsets = offsets.contiguous()
+    if not sort_by_cell or points.shape[1] == 0:
+        return TransformGridRagged.apply(points, theta, offsets, params)
+    total = points.shape[1]
+    nC = N.num_cells(params.nc)
+    pos = torch.arange(total, device=points.device)
+    set_id = torch.searchsorted(offsets, pos, right=True) - 1
+    cell = findcellidx(params.ndim, points, params.nc)
+    perm = torch.sort(set_id * nC + cell, stable=True).indices
+    inv = torch.empty_like(perm)
+    inv[perm] = pos
+    out = TransformGridRagged.apply(points[:, perm], theta, offsets, params)
+    return out[:, inv]
+
+
 def findcellidx(ndim, p, nc):
     """Cell index of each column of p [ndim, nP] (int64), with the reference's
     C++/CUDA lookup rules (libcpab/core/cpab_ops.cpp:26-190)."""

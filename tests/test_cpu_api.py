@@ -93,3 +93,19 @@ def test_exact_flow_oracle_matches_closed_form_1d(nc, zb):
         A = (B @ theta[k]).reshape(nc[0], 2)
         ref = np.array([_closed_form_1d(A, float(x), nc[0]) for x in pts[0]])
         assert np.abs(ode[k, 0] - ref).max() <= 1e-8
+
+
+def test_ragged_points_argument_checks():
+    from libcpab_gb300 import Cpab, functions
+    T = Cpab([3, 3], backend='pytorch', device='gpu')
+    pts = torch.zeros(2, 20)
+    off = torch.tensor([0, 8, 20])
+    theta = torch.zeros(2, T.get_theta_dim())
+    with pytest.raises(ValueError):                 # CPU tensors: no fallback
+        functions.transform_grid_ragged(pts, off, theta, T.params)
+    meta = lambda *s, **k: torch.empty(*s, device='meta', **k)
+    for p, o, th in ((meta(3, 20), meta(3, dtype=torch.int64), meta(2, 4)),
+                     (meta(2, 20), meta(3, dtype=torch.int32), meta(2, 4)),
+                     (meta(2, 20), meta(3, dtype=torch.int64), meta(3, 4))):
+        with pytest.raises(ValueError):
+            functions._check_ragged_points(p, o, th, T.params)
