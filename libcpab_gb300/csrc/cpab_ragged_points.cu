@@ -101,7 +101,7 @@ __host__ __device__ inline size_t points_adjoint_smem(int nC, int nsteps, int bl
 }
 
 template <int N, int MODE, typename CT>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
     k_ragged_points_adjoint(Tess t, int nsteps, Steps st, int S, const long long *__restrict__ off,
                             const int *__restrict__ tile_off, int ppt,
                             const float *__restrict__ table, long long total,
