@@ -145,7 +145,9 @@ class Interpolate(torch.autograd.Function):
 
 class TransformData(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, data, theta, params, outsize):
+    def forward(ctx, data, theta, params, outsize, upload=None):
+        # upload: a host_io.HostUpload whose tensor is `data`, still arriving
+        # in batch chunks; chunk k is integrated once its copy has landed
         data_c = data.detach().to(torch.float32).contiguous()
         theta_c = theta.detach().to(torch.float32).contiguous()
         dev = data.device
@@ -156,8 +158,24 @@ class TransformData(torch.autograd.Function):
         mode = _mode(params)
         needs_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
         save_grid = needs_grad and mode == N.GRAD_REFERENCE
-        out, grid = N.transform_data(params.nc, params.nstepsolver, lin, outsize, E, data_c,
-                                     save_grid=save_grid, ties=_ties(params))
+        if upload is None:
+            out, grid = N.transform_data(params.nc, params.nstepsolver, lin, outsize, E, data_c,
+                                         save_grid=save_grid, ties=_ties(params))
+        else:
+            if data_c.data_ptr() != upload.tensor.data_ptr():
+                raise ValueError('data must be the uploaded tensor')
+            nb, C = data_c.shape[0], data_c.shape[1]
+            nP = 1
+            for o in outsize:
+                nP *= int(o)
+            out = torch.empty((nb, C, *outsize), device=dev, dtype=torch.float32)
+            grid = torch.empty((nb, params.ndim, nP), device=dev, dtype=torch.float32) \
+                if save_grid else None
+            for k, (a, b) in enumerate(upload.bounds):
+                upload.wait(k)
+                N.transform_data(params.nc, params.nstepsolver, lin, outsize, E[a:b],
+                                 data_c[a:b], save_grid=save_grid, ties=_ties(params),
+                                 out=out[a:b], grid=grid[a:b] if save_grid else None)
         ctx.save_for_backward(data_c, lin, A, E, grid)
         ctx.params = params
         ctx.outsize = outsize
@@ -171,12 +189,12 @@ class TransformData(torch.autograd.Function):
         params = ctx.params
         want_d, want_t = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
         if not (want_d or want_t):
-            return None, None, None, None
+            return None, None, None, None, None
         ddata, dtheta = N.transform_data_backward(
             params.nc, params.nstepsolver, ctx.mode, lin, ctx.outsize, A, E, grid, data,
             _basis(params, data.device), grad.to(torch.float32).contiguous(), want_ddata=want_d,
             ties=_ties(params))
-        return ddata, (dtheta if want_t else None), None, None
+        return ddata, (dtheta if want_t else None), None, None, None
 
 
 class TransformDataRagged(torch.autograd.Function):

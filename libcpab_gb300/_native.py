@@ -271,7 +271,10 @@ def interpolate_backward(data, grid, outsize, grad_out, want_ddata=True, want_dg
     return ddata, dgrid
 
 
-def transform_data(nc, nsteps, lin, outsize, E, data, save_grid=False, ties=None):
+def transform_data(nc, nsteps, lin, outsize, E, data, save_grid=False, ties=None, out=None,
+                   grid=None):
+    """Fused forward; out ([nb, C, *outsize]) and grid ([nb, ndim, prod(outsize)], only with
+    save_grid) may be given (contiguous, e.g. batch slices of larger buffers)."""
     _require(lin, 'lin')
     _require(E, 'E')
     _require(data, 'data')
@@ -280,10 +283,21 @@ def transform_data(nc, nsteps, lin, outsize, E, data, save_grid=False, ties=None
     nP = 1
     for o in outsize:
         nP *= int(o)
-    out = torch.empty((nb, C, *[int(o) for o in outsize]), device=data.device,
-                      dtype=torch.float32)
-    grid = torch.empty((nb, ndim, nP), device=data.device, dtype=torch.float32) \
-        if save_grid else None
+    oshape = (nb, C, *[int(o) for o in outsize])
+    if out is None:
+        out = torch.empty(oshape, device=data.device, dtype=torch.float32)
+    else:
+        _require(out, 'out')
+        if tuple(out.shape) != oshape:
+            raise ValueError('out must be %s' % (oshape,))
+    if not save_grid:
+        grid = None
+    elif grid is None:
+        grid = torch.empty((nb, ndim, nP), device=data.device, dtype=torch.float32)
+    else:
+        _require(grid, 'grid')
+        if tuple(grid.shape) != (nb, ndim, nP):
+            raise ValueError('grid must be %s' % ((nb, ndim, nP),))
     _check(load().cpab_transform_data(ndim, _ints(nc), int(nsteps), _ptr(lin), _ints(outsize),
                                       _ptr(E), nb, _ptr(data), C, _ints(data.shape[2:]),
                                       _ptr(out), _ptr(grid), _ptr(ties), _stream(data.device)))

@@ -56,6 +56,8 @@ struct Tess {
     float clamp3[3];  // 3D clamp limits (float)(nc*inc - 1e-8), z uses inc_x
     int band[3];      // 1 if (float)(nc*inc) > nc*inc: floats in [nc*inc, wlim) exist
     int band_any;     // band[0] | band[1] | band[2]
+    int tier2;        // 2D second-tier tie decisions apply (square cells, see cell_2d_tier2)
+    int pow2;         // nc[0] and nc[1] are powers of two: p / inc == p * nc exactly
     float ncf[3];     // nc as float
 };
 
@@ -92,6 +94,12 @@ inline int tess_init(int ndim, const int *nc, Tess *t) {
         cells *= n;
     }
     t->nC = (int)(cells * (ndim == 1 ? 1 : ndim == 2 ? 4 : 5));
+    // cell_2d_tier2 needs one divisor for both axes and no float strictly
+    // between wlim - 1e-9 (the reference's clamp) and wlim
+    t->tier2 = ndim == 2 && t->inc[0] == t->inc[1];
+    for (int j = 0; j < 2; ++j)
+        t->tier2 &= (double)nextafterf(t->wlim[j], 0.f) <= (double)t->wlim[j] - 0.000000001;
+    t->pow2 = ndim == 2 && (t->nc[0] & (t->nc[0] - 1)) == 0 && (t->nc[1] & (t->nc[1] - 1)) == 0;
     if (ndim == 3) {
         t->clamp3[0] = (float)((double)((float)nc[0] * t->inc[0]) - 1e-8);
         t->clamp3[1] = (float)((double)((float)nc[1] * t->inc[1]) - 1e-8);
@@ -218,6 +226,9 @@ CPAB_HD inline void split_exact(float p, float inc, float rinc, float &fi, float
 // |p * rinc| below this keeps every integer in split_exact exact.
 constexpr float kSplitLimit = 2097152.0f;   // 2^21
 
+// cell_2d_fast's code for "a triangle decision is within its margin".
+constexpr int kTie2 = -2;
+
 // Margin of the FP32 sub-cell tests.  A sub-cell coordinate rem*rinc differs
 // from the reference's double rem/inc by at most 2^-22; a two-term test then
 // carries an error below (1+|x|+|y|) 2^-21 and a three-term test below
@@ -226,7 +237,8 @@ constexpr float kMargin2 = 1.9073486328125e-06f;   // 2^-19
 constexpr float kMargin3 = 3.814697265625e-06f;    // 2^-18
 
 // FP32 2D lookup with the reference's semantics for every finite point;
-// returns -1 when a decision is within its error margin.
+// returns kTie2 when a triangle decision is within its error margin (the
+// second tier may decide it) and -1 in the other deferred cases.
 //
 // Outside the domain the reference applies its left/right/above/below rules
 // (cpab_ops.cpp:57-90).  Each of them is the in-square triangle test applied
@@ -254,17 +266,111 @@ CPAB_HD inline int cell_2d_fast(float px, float py, const Tess &t) {
     const float y = fmaf(rj, t.rinc[1], fj - cj);
     const float dxy = x - y, sxy = (x + y) - 1.f;
     const float m = kMargin2 * ((1.f + fabsf(x)) + fabsf(y));
-    if (!(fabsf(dxy) > m) || !(fabsf(sxy) > m)) return -1;
+    if (!(fabsf(dxy) > m) || !(fabsf(sxy) > m)) return kTie2;
     // triangle: 0 (dxy >= 0, sxy <= 0), 1 (dxy >= 0, sxy > 0), 2 (dxy < 0,
     // sxy > 0), 3 (dxy < 0, sxy <= 0) = (sxy > 0) xor (dxy < 0 ? 3 : 0)
     const int tri = (sxy > 0.f ? 1 : 0) ^ (dxy < 0.f ? 3 : 0);
     return small_float_to_int(4.f * fmaf(cj, t.ncf[0], ci)) + tri;
 }
 
+// Second tier for triangle decisions inside the FP32 margin, for square
+// cells (inc_x == inc_y, Tess::tier2).  Trajectories that sit on a tie for
+// many steps (zero-boundary domain corners are fixed points up to ~1e-17
+// drift) would otherwise take the FP64 replica at every step.  It follows the
+// reference's branch order (cpab_ops.cpp:57-98) and decides each comparison
+// exactly where that is provable, else returns -1 (FP64 replica):
+//  * fx < fy, i.e. rx/ix < ry/iy, and py/iy < px/ix: with one divisor the
+//    correctly rounded double quotients of two distinct floats keep their
+//    order (relative gap >= 2^-24 >> 2^-53), so the float comparison decides;
+//  * 1 - fx < fy: the reference's double evaluation is within 3*2^-53 of
+//    1 - (rx + ry)/ix; T = (ix - rx) - ry in double is within 2^-52 ix of its
+//    exact value, so |T| > 2^-48 ix decides the test by the sign of T;
+//  * the out-of-domain rules outside in x and y (cpab_ops.cpp:59-82), e.g.
+//    py/iy - ny > -px/ix: multiplied by ix = iy they compare
+//    D = px + py - ny*iy (or py - px - (ny - nx) ix, px + py - nx ix) with 0.
+//    Each side of the reference's comparison carries at most two roundings
+//    (2^-52 relative); D evaluated in double carries at most 2^-52 of
+//    |px| + |py| + (nx + ny) ix, so |D| above 2^-48 of that decides by its
+//    sign.  Identical evaluations (px == py, nx == ny) compare equal.
+//  * with power-of-two cell counts (Tess::pow2) division by inc is
+//    multiplication by nc, exact in double, so a comparison that the bounds
+//    above leave open is evaluated with the reference's own operations.
+// rx and ry are split_exact's float remainders, equal to the reference's
+// fmod for 0 < p < wlim (and p <= wlim - 1e-9 there, by Tess::tier2).  Called
+// only after cell_2d_fast returned kTie2, i.e. past the band and range checks,
+// so the clamped split is the reference's square.
+static CPAB_HD __noinline__ int cell_2d_tier2(float px, float py, const Tess &t) {
+    float fi, ri, fj, rj;
+    split_exact(px, t.inc[0], t.rinc[0], fi, ri);
+    split_exact(py, t.inc[1], t.rinc[1], fj, rj);
+    const float ci = fminf(fmaxf(fi, 0.f), t.ncf[0] - 1.f);
+    const float cj = fminf(fmaxf(fj, 0.f), t.ncf[1] - 1.f);
+    const int c = small_float_to_int(4.f * fmaf(cj, t.ncf[0], ci));
+    const double kEps = 3.552713678800501e-15;   // 2^-48
+    const double nix = (double)t.nc[0] * (double)t.inc[0], niy = (double)t.nc[1] * (double)t.inc[1];
+    const double scale = (fabs((double)px) + fabs((double)py)) + (nix + niy);
+    int tri;
+    if (px <= 0.f) {
+        if (py <= 0.f) {
+            tri = (py < px) ? 0 : 3;
+        } else if (py >= t.wlim[1]) {                 // py/iy - ny > -px/ix ?
+            const double D = ((double)px + (double)py) - niy;
+            if (fabs(D) > kEps * scale) tri = D > 0.0 ? 2 : 3;
+            else if (t.pow2) tri = ((double)py * t.nc[1] - t.nc[1] > -((double)px * t.nc[0])) ? 2 : 3;
+            else return -1;
+        } else {
+            tri = 3;
+        }
+    } else if (px >= t.wlim[0]) {
+        if (py <= 0.f) {                              // -py/iy > px/ix - nx ?
+            const double D = ((double)px + (double)py) - nix;
+            if (fabs(D) > kEps * scale) tri = D < 0.0 ? 0 : 1;
+            else if (t.pow2) tri = (-((double)py * t.nc[1]) > (double)px * t.nc[0] - t.nc[0]) ? 0 : 1;
+            else return -1;
+        } else if (py >= t.wlim[1]) {                 // py/iy - ny > px/ix - nx ?
+            if (px == py && t.nc[0] == t.nc[1]) {
+                tri = 1;
+            } else {
+                const double D = ((double)py - (double)px) -
+                                 ((double)t.nc[1] - (double)t.nc[0]) * (double)t.inc[0];
+                if (fabs(D) > kEps * scale) tri = D > 0.0 ? 2 : 1;
+                else if (t.pow2)
+                    tri = ((double)py * t.nc[1] - t.nc[1] > (double)px * t.nc[0] - t.nc[0]) ? 2 : 1;
+                else return -1;
+            }
+        } else {
+            tri = 1;
+        }
+    } else if (py <= 0.f) {
+        tri = 0;
+    } else if (py >= t.wlim[1]) {
+        tri = 2;
+    } else {
+        const double T = ((double)t.inc[0] - (double)ri) - (double)rj;
+        bool s;                                                                   // 1 - fx < fy
+        if (fabs(T) > kEps * (double)t.inc[0]) s = T < 0.0;
+        else if (t.pow2) s = 1.0 - (double)ri * t.nc[0] < (double)rj * t.nc[1];
+        else return -1;
+        tri = (ri < rj) ? (s ? 2 : 3) : (s ? 1 : 0);
+    }
+    return c + tri;
+}
+
+// FP32 decision of both tiers (-1: the FP64 replica must decide).
+CPAB_HD inline int cell_2d_fp32(float px, float py, const Tess &t) {
+    const int c = cell_2d_fast(px, py, t);
+    if (c >= 0 || c != kTie2 || !t.tier2) return c >= 0 ? c : -1;
+    return cell_2d_tier2(px, py, t);
+}
+
 __device__ __forceinline__ int cell_2d(float px, float py, const Tess &t,
                                        unsigned long long *ties) {
-    const int c = cell_2d_fast(px, py, t);
+    int c = cell_2d_fast(px, py, t);
     if (c >= 0) return c;
+    if (c == kTie2 && t.tier2) {
+        c = cell_2d_tier2(px, py, t);
+        if (c >= 0) return c;
+    }
     if (ties) atomicAdd(ties, 1ull);
     return cell_2d_exact(px, py, t);
 }

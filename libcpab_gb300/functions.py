@@ -184,6 +184,32 @@ def transform_data(data, theta, params, outsize):
     return TransformData.apply(data, theta, params, outsize)
 
 
+def transform_data_from_host(data, theta, params, outsize, chunks=4, requires_grad=False):
+    """transform_data for a batch held in host memory: the batch is copied to
+    the GPU in `chunks` slices on a side stream and the fused forward of each
+    slice starts as soon as it has arrived (host_io.HostUpload), so the copy
+    overlaps with the integration.  Same result as
+    transform_data(data.cuda(), theta, params, outsize).  Returns (out, data
+    on the device); with requires_grad the device copy is a leaf whose .grad
+    receives d(data)."""
+    from .host_io import HostUpload
+    _require_cuda(theta)
+    if data.is_cuda:
+        raise ValueError('transform_data_from_host takes a host tensor (got %s)' % data.device)
+    outsize = tuple(int(o) for o in outsize[:params.ndim])
+    if data.dim() != params.ndim + 2:
+        raise ValueError('data must be [n_batch, n_channels, *%dD size]' % params.ndim)
+    if data.shape[0] != theta.shape[0]:
+        raise ValueError('data and theta must have the same batch size (%d vs %d)'
+                         % (data.shape[0], theta.shape[0]))
+    if params.numeric_grad or getattr(params, 'integration', 'fixed_step') == 'exact':
+        dev = HostUpload(data, theta.device).wait().requires_grad_(requires_grad)
+        return transform_data(dev, theta, params, outsize), dev
+    up = HostUpload(data, theta.device, chunks=chunks)
+    dev = up.tensor.requires_grad_(requires_grad)
+    return TransformData.apply(dev, theta, params, outsize, up), dev
+
+
 def _check_ragged(values, offsets, theta, params):
     _require_cuda(values, offsets, theta)
     if params.ndim != 1:

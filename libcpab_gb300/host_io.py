@@ -1,0 +1,89 @@
+"""Host-to-device input staging that overlaps with the integration kernels.
+
+A caller whose inputs live in (pinned) host memory would otherwise copy a
+whole batch to the GPU before the first kernel starts.  HostUpload issues the
+copy on a side stream in batch chunks and records one event per chunk;
+transform_data_from_host (functions.py) starts the fused forward of chunk k
+as soon as chunk k has arrived, so the copy of the rest of the batch runs
+under the forward of the first chunks.  Everything stays stream-ordered (no
+host synchronisation), so it can also be captured in a CUDA graph.
+"""
+from __future__ import annotations
+
+import threading
+
+import torch
+
+_streams = {}
+_lock = threading.Lock()
+
+
+def copy_stream(device) -> torch.cuda.Stream:
+    """One side stream per device for host-to-device copies."""
+    device = torch.device(device)
+    idx = device.index if device.index is not None else torch.cuda.current_device()
+    with _lock:
+        st = _streams.get(idx)
+        if st is None:
+            st = torch.cuda.Stream(device=torch.device('cuda', idx))
+            _streams[idx] = st
+    return st
+
+
+def chunk_bounds(n: int, chunks: int):
+    """[(a, b), ...]: n rows in at most `chunks` nearly equal consecutive parts."""
+    chunks = max(1, min(int(chunks), n)) if n > 0 else 1
+    base, extra = divmod(n, chunks)
+    out, a = [], 0
+    for k in range(chunks):
+        b = a + base + (1 if k < extra else 0)
+        out.append((a, b))
+        a = b
+    return out
+
+
+class HostUpload:
+    """Copy a host tensor to `device` in `chunks` slices of its first axis on
+    the copy stream.  `tensor` is the device tensor (usable once the matching
+    event has been waited for); wait(k) makes the current stream wait for
+    chunk k, wait() for all of them, and returns the tensor."""
+
+    def __init__(self, host: torch.Tensor, device, chunks: int = 1, dtype=torch.float32):
+        if host.is_cuda:
+            raise ValueError('HostUpload takes a host tensor')
+        device = torch.device(device)
+        host = host.detach()
+        if host.dtype != dtype:
+            host = host.to(dtype)
+        host = host.contiguous()
+        if not host.is_pinned():
+            # a pageable source would make the copy synchronous
+            host = host.pin_memory()
+        self.host = host
+        cur = torch.cuda.current_stream(device)
+        cs = copy_stream(device)
+        n = host.shape[0] if host.dim() > 0 else 1
+        self.bounds = chunk_bounds(n, chunks) if host.dim() > 0 else [(0, 1)]
+        self.events = []
+        with torch.cuda.stream(cs):
+            # allocated on the copy stream: the allocator hands it a block
+            # whose earlier users are ordered before this copy, so the copy
+            # need not wait for the current stream's queued kernels
+            self.tensor = torch.empty(host.shape, dtype=dtype, device=device)
+            for a, b in self.bounds:
+                if host.dim() > 0:
+                    self.tensor[a:b].copy_(host[a:b], non_blocking=True)
+                else:
+                    self.tensor.copy_(host, non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(cs)
+                self.events.append(ev)
+        # consumers run on the current stream: the block is reused only after
+        # their queued work is done
+        self.tensor.record_stream(cur)
+
+    def wait(self, k: int | None = None) -> torch.Tensor:
+        cur = torch.cuda.current_stream(self.tensor.device)
+        for ev in (self.events if k is None else [self.events[k]]):
+            cur.wait_event(ev)
+        return self.tensor

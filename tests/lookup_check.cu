@@ -3,7 +3,7 @@
 //
 // usage: lookup_check <in.bin> <out.bin>
 //   in:  int32 ndim, int32 nc[3], int64 n, float32 points[ndim][n]
-//   out: int32 fast[n] (-1 where the FP32 path defers), int32 exact[n]
+//   out: int32 fast[n] (-1 where the FP32 tiers defer), int32 exact[n]
 #include <cstdio>
 #include <cstdint>
 #include <vector>
@@ -29,7 +29,7 @@ int main(int argc, char **argv) {
         if (ndim == 1) {
             fast[i] = exact[i] = cpab::cell_1d(x, t);
         } else if (ndim == 2) {
-            fast[i] = cpab::cell_2d_fast(x, y, t);
+            fast[i] = cpab::cell_2d_fp32(x, y, t);
             exact[i] = cpab::cell_2d_exact(x, y, t);
         } else {
             fast[i] = cpab::cell_3d_fast(x, y, z, t);

@@ -128,3 +128,46 @@ def test_fp32_lookup_agrees_with_fp64_replica_and_oracle(nc, harness, tmp_path, 
         f3, e3 = run(harness, tmp_path, nc, O)
         assert np.array_equal(f3[f3 >= 0], e3[f3 >= 0])
         assert (f3 < 0).mean() < 1e-3
+
+
+@pytest.mark.parametrize('nc', [[3, 3], [8, 8], [4, 4], [7, 5], [5, 5], [6, 6], [16, 16]])
+def test_second_tier_ties_2d(nc, harness, tmp_path):
+    """2D points on or within a few ulp of the triangle diagonals, and the
+    zero-boundary domain corners with the ~1e-17 drift their trajectories
+    have: wherever the FP32 tiers answer they equal the FP64 replica, and for
+    square cells they answer the corner points (fixed points of the flow, a
+    tie at every step) without the replica."""
+    rng = np.random.default_rng(sum(nc) * 31 + 5)
+    inc = np.float32(1.0) / np.float32(nc[0])
+    m = 40000
+    # main diagonal px == py and anti-diagonal px + py == inc of square (0, 0),
+    # exact and +-1..2 ulp
+    a = rng.uniform(0, float(inc), m).astype(np.float32)
+    b = rng.uniform(float(inc) / 2, float(inc), m).astype(np.float32)
+    anti = (inc - b).astype(np.float32)                 # exact (Sterbenz)
+    pts = [np.stack([a, a]), np.stack([b, anti])]
+    for k in (1, 2):
+        pts.append(np.stack([a, np.nextafter(a, np.float32(2)) if k == 1 else
+                             np.nextafter(np.nextafter(a, np.float32(-2)), np.float32(-2))]))
+        pts.append(np.stack([b, np.nextafter(anti, np.float32(2 * k - 3))]))
+    # the diagonals of other squares: same remainder in both coordinates
+    i = rng.integers(0, nc[0], m)
+    j = rng.integers(0, nc[1], m)
+    r = rng.uniform(0, 1, m)
+    pts.append(np.stack([((i + r) / nc[0]).astype(np.float32),
+                         ((j + r) / nc[1]).astype(np.float32)]))
+    # domain corners with drift
+    drift = np.array([0.0, -0.0, 1e-30, -1e-30, 1e-18, -1e-18, 1.3e-17, -7e-17, 1e-12, 1e-7],
+                     dtype=np.float32)
+    cx = rng.integers(0, 2, m).astype(np.float32)
+    cy = rng.integers(0, 2, m).astype(np.float32)
+    corner = np.stack([cx + rng.choice(drift, m), cy + rng.choice(drift, m)]).astype(np.float32)
+    pts.append(corner)
+    P = np.concatenate(pts, axis=1)
+    fast, exact = run(harness, tmp_path, nc, P)
+    answered = fast >= 0
+    bad = np.nonzero(answered & (fast != exact))[0]
+    assert bad.size == 0, 'FP32 tiers wrong at %s' % P[:, bad[:5]].T
+    fc, _ = run(harness, tmp_path, nc, corner)
+    if nc[0] == nc[1]:
+        assert (fc >= 0).mean() > 0.99, (fc >= 0).mean()
