@@ -235,15 +235,13 @@ def run_gb300(args):
     graph_matches = bool(torch.equal(g_dth, e_dth) and torch.equal(g_loss, e_loss))
 
     # e2e through the public API with host buffers: H2D inputs, D2H loss + dtheta.
-    # transform_data_from_host copies the images in 4 batch chunks on a side
-    # stream and starts each chunk's forward when it has landed; the target
-    # follows on the same copy stream, under the forward
+    # transform_data_from_host copies the images on a side stream while the
+    # trajectories are integrated; the target follows on the same copy stream
     from libcpab_gb300.host_io import HostUpload
 
     def step_e2e():
         th = theta_h.to(device, non_blocking=True).requires_grad_(True)
-        out, dd = T.transform_data_from_host(data_h, th, [SIZE, SIZE], chunks=4,
-                                             requires_grad=True)
+        out, dd = T.transform_data_from_host(data_h, th, [SIZE, SIZE], requires_grad=True)
         tg = HostUpload(target_h, device).wait()
         loss = F.mse_loss(out, tg)
         loss.backward()
@@ -348,9 +346,10 @@ def run_gb300(args):
                                                                               graph_matches)},
             'e2e': {'value': e2e_value, 'unit': 'points/s', 'h2d_bytes_per_step': h2d,
                     'd2h_bytes_per_step': d2h, 'ms_per_step': ms_e2e_max,
-                    'path': 'Cpab.transform_data_from_host (images copied in 4 batch chunks '
-                            'under the fused forward), target copied on the same side stream, '
-                            'F.mse_loss, backward, loss + dtheta read back; eager',
+                    'path': 'Cpab.transform_data_from_host (images copied on a side stream '
+                            'while the trajectories are integrated, then sampled), target '
+                            'copied on the same side stream, F.mse_loss, backward, loss + '
+                            'dtheta read back; eager',
                     'serial_copies_ms_per_step': ms_e2e_serial,
                     'same_result_as_serial': e2e_matches},
             'gpu_launches': 4 * args.steps,

@@ -184,6 +184,25 @@ CPAB_API int cpab_transform_data(int ndim, const int *nc, int nsteps, const floa
                         const int *size, float *out, float *grid_out,
                         unsigned long long *ties, void *stream);
 
+/*
+ * The two halves of cpab_transform_data, for callers whose images are still
+ * arriving (e.g. a host-to-device copy on another stream) while the
+ * trajectories are integrated.  cpab_transform_grid_image writes the
+ * transformed meshgrid as [nb, ndim, prod(outsize)] in image order (the
+ * grid_out of cpab_transform_data; it needs no image); cpab_sample_grid then
+ * samples data at that grid into out (image layout).  Together they give
+ * cpab_transform_data's output bit for bit.  No counterpart in the
+ * reference (its transform_data, libcpab/cpab.py:304-331, runs
+ * uniform_meshgrid, transform_grid and interpolate as separate passes in
+ * meshgrid order).
+ */
+CPAB_API int cpab_transform_grid_image(int ndim, const int *nc, int nsteps, const float *lin,
+                                       const int *outsize, const float *E, int nb,
+                                       float *grid_out, unsigned long long *ties, void *stream);
+
+CPAB_API int cpab_sample_grid(int ndim, const float *data, int nb, int C, const int *size,
+                              const float *grid, const int *outsize, float *out, void *stream);
+
 CPAB_API size_t cpab_transform_data_backward_workspace(int ndim, const int *nc, int nsteps, int mode,
                                               const int *outsize, int nb);
 

@@ -146,8 +146,9 @@ class Interpolate(torch.autograd.Function):
 class TransformData(torch.autograd.Function):
     @staticmethod
     def forward(ctx, data, theta, params, outsize, upload=None):
-        # upload: a host_io.HostUpload whose tensor is `data`, still arriving
-        # in batch chunks; chunk k is integrated once its copy has landed
+        # upload: a host_io.HostUpload whose tensor is `data`, still arriving:
+        # the trajectories are integrated first (they need no image), then the
+        # stream waits for the copy and samples (split forward, same bits)
         data_c = data.detach().to(torch.float32).contiguous()
         theta_c = theta.detach().to(torch.float32).contiguous()
         dev = data.device
@@ -164,18 +165,12 @@ class TransformData(torch.autograd.Function):
         else:
             if data_c.data_ptr() != upload.tensor.data_ptr():
                 raise ValueError('data must be the uploaded tensor')
-            nb, C = data_c.shape[0], data_c.shape[1]
-            nP = 1
-            for o in outsize:
-                nP *= int(o)
-            out = torch.empty((nb, C, *outsize), device=dev, dtype=torch.float32)
-            grid = torch.empty((nb, params.ndim, nP), device=dev, dtype=torch.float32) \
-                if save_grid else None
-            for k, (a, b) in enumerate(upload.bounds):
-                upload.wait(k)
-                N.transform_data(params.nc, params.nstepsolver, lin, outsize, E[a:b],
-                                 data_c[a:b], save_grid=save_grid, ties=_ties(params),
-                                 out=out[a:b], grid=grid[a:b] if save_grid else None)
+            grid = N.transform_grid_image(params.nc, params.nstepsolver, lin, outsize, E,
+                                          ties=_ties(params))
+            upload.wait()
+            out = N.sample_grid(data_c, grid, outsize)
+            if not save_grid:
+                grid = None
         ctx.save_for_backward(data_c, lin, A, E, grid)
         ctx.params = params
         ctx.outsize = outsize

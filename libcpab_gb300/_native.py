@@ -43,6 +43,8 @@ _SIGS = {
                                   _i),
     'cpab_transform_data': ([_i, _c_int_p, _i, _vp, _c_int_p, _vp, _i, _vp, _i, _c_int_p, _vp,
                              _vp, _vp, _vp], _i),
+    'cpab_transform_grid_image': ([_i, _c_int_p, _i, _vp, _c_int_p, _vp, _i, _vp, _vp, _vp], _i),
+    'cpab_sample_grid': ([_i, _vp, _i, _i, _c_int_p, _vp, _c_int_p, _vp, _vp], _i),
     'cpab_transform_data_backward_workspace': ([_i, _c_int_p, _i, _i, _c_int_p, _i], _sz),
     'cpab_transform_data_backward': ([_i, _c_int_p, _i, _i, _vp, _c_int_p, _vp, _vp, _vp, _i, _vp,
                                       _i, _c_int_p, _vp, _i, _vp, _vp, _vp, _vp, _sz, _vp, _vp],
@@ -302,6 +304,37 @@ def transform_data(nc, nsteps, lin, outsize, E, data, save_grid=False, ties=None
                                       _ptr(E), nb, _ptr(data), C, _ints(data.shape[2:]),
                                       _ptr(out), _ptr(grid), _ptr(ties), _stream(data.device)))
     return out, grid
+
+
+def transform_grid_image(nc, nsteps, lin, outsize, E, ties=None):
+    """The integration half of transform_data: the transformed meshgrid of lin
+    for every table, [nb, ndim, prod(outsize)] in image order."""
+    _require(lin, 'lin')
+    _require(E, 'E')
+    ndim = len(nc)
+    nb = E.shape[0]
+    nP = 1
+    for o in outsize:
+        nP *= int(o)
+    grid = torch.empty((nb, ndim, nP), device=E.device, dtype=torch.float32)
+    _check(load().cpab_transform_grid_image(ndim, _ints(nc), int(nsteps), _ptr(lin),
+                                            _ints(outsize), _ptr(E), nb, _ptr(grid), _ptr(ties),
+                                            _stream(E.device)))
+    return grid
+
+
+def sample_grid(data, grid, outsize):
+    """The sampling half of transform_data: data [nb, C, *size] at an
+    image-order grid from transform_grid_image."""
+    _require(data, 'data')
+    _require(grid, 'grid')
+    ndim = grid.shape[1]
+    nb, C = data.shape[0], data.shape[1]
+    out = torch.empty((nb, C, *[int(o) for o in outsize]), device=data.device,
+                      dtype=torch.float32)
+    _check(load().cpab_sample_grid(ndim, _ptr(data), nb, C, _ints(data.shape[2:]), _ptr(grid),
+                                   _ints(outsize), _ptr(out), _stream(data.device)))
+    return out
 
 
 def transform_data_backward(nc, nsteps, mode, lin, outsize, A, E, grid_saved, data, basis,

@@ -215,14 +215,14 @@ class Cpab(object):
         self._check_type(theta); self._check_device(theta)
         return self.backend.transform_data(data, theta, self.params, outsize)
 
-    def transform_data_from_host(self, data, theta, outsize, chunks=4, requires_grad=False):
+    def transform_data_from_host(self, data, theta, outsize, requires_grad=False):
         """transform_data with the batch in (pinned) host memory (extension):
-        the copy to the GPU runs in batch chunks under the fused forward of
-        the chunks already copied.  Returns (output, the device copy of data);
-        with requires_grad the device copy receives d(data) in .grad."""
+        the copy to the GPU runs under the integration of the trajectories.
+        Returns (output, the device copy of data); with requires_grad the
+        device copy receives d(data) in .grad."""
         self._check_type(theta); self._check_device(theta)
         return self.backend.transform_data_from_host(data, theta, self.params, outsize,
-                                                     chunks=chunks, requires_grad=requires_grad)
+                                                     requires_grad=requires_grad)
 
     def transform_data_ragged(self, values, offsets, theta):
         """Ragged batch of 1D series (extension; no reference counterpart):

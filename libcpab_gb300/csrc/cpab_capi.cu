@@ -291,6 +291,38 @@ int cpab_transform_data(int ndim, const int *nc, int nsteps, const float *lin,
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "transform_data launch");
 }
 
+int cpab_transform_grid_image(int ndim, const int *nc, int nsteps, const float *lin,
+                              const int *outsize, const float *E, int nb, float *grid_out,
+                              unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if ((rc = check_geo(ndim, outsize, outsize, nb))) return rc;
+    if (nb < 0) return fail(CPAB_ERR_ARGUMENT, "invalid nb");
+    if (nb == 0) return CPAB_OK;
+    if (!lin || !E || !grid_out) return fail(CPAB_ERR_ARGUMENT, "lin, E or grid_out is NULL");
+    cudaError_t e = launch_transform_data(t, nsteps, lin, outsize, E, nb, nullptr, 0, outsize,
+                                          nullptr, grid_out, ties, device_error_word(),
+                                          as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "transform_grid_image launch");
+}
+
+int cpab_sample_grid(int ndim, const float *data, int nb, int C, const int *size,
+                     const float *grid, const int *outsize, float *out, void *stream) {
+    g_err[0] = 0;
+    if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3");
+    int rc;
+    if ((rc = check_geo(ndim, size, outsize, nb))) return rc;
+    if (nb < 0 || C < 1) return fail(CPAB_ERR_ARGUMENT, "invalid nb or C");
+    if (nb == 0) return CPAB_OK;
+    if (!data || !grid || !out) return fail(CPAB_ERR_ARGUMENT, "data, grid or out is NULL");
+    cudaError_t e = launch_sample_grid(ndim, grid, nb, data, C, size, outsize, out,
+                                       as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "sample_grid launch");
+}
+
 size_t cpab_transform_data_backward_workspace(int ndim, const int *nc, int nsteps, int mode,
                                               const int *outsize, int nb) {
     g_err[0] = 0;

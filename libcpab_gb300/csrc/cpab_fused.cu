@@ -83,15 +83,51 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int j = 0; j < PPT; ++j) {
         if (o[j] >= g.nP) continue;
-        const Corner<N> cr = corners<N>(p[j], g);
-        for (int c = 0; c < C; ++c)
-            out[((long long)b * C + c) * g.nP + o[j]] =
-                lerp_corners<N>(data + ((long long)b * C + c) * g.nD, cr);
+        if (C > 0) {   // C == 0: integrate only (grid_out), sampled later by k_sample_grid
+            const Corner<N> cr = corners<N>(p[j], g);
+            for (int c = 0; c < C; ++c)
+                out[((long long)b * C + c) * g.nP + o[j]] =
+                    lerp_corners<N>(data + ((long long)b * C + c) * g.nD, cr);
+        }
         if (grid_out) {
 #pragma unroll
             for (int r = 0; r < N; ++r) grid_out[((long long)b * N + r) * g.nP + o[j]] = p[j][r];
         }
     }
+}
+
+// Sampling half of a split transform_data forward: the epilogue of
+// k_transform_data applied to a grid saved in image order (grid_out of a
+// C = 0 launch), so that the images can arrive while the trajectories are
+// integrated.  Same arithmetic as the fused epilogue: bit-identical output.
+template <int N>
+__global__ void __launch_bounds__(256)
+    k_sample_grid(Geo g, const float *__restrict__ grid, int C, const float *__restrict__ data,
+                  float *__restrict__ out) {
+    const int b = blockIdx.y;
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= g.nP) return;
+    float p[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) p[r] = __ldg(grid + ((long long)b * N + r) * g.nP + o);
+    const Corner<N> cr = corners<N>(p, g);
+    for (int c = 0; c < C; ++c)
+        out[((long long)b * C + c) * g.nP + o] =
+            lerp_corners<N>(data + ((long long)b * C + c) * g.nD, cr);
+}
+
+cudaError_t launch_sample_grid(int ndim, const float *grid, int nb, const float *data, int C,
+                               const int *size, const int *outsize, float *out, cudaStream_t s) {
+    const Geo g = make_geo(ndim, size, outsize);
+    if ((long long)nb * g.nP == 0) return cudaSuccess;
+    if (nb > 65535) return cudaErrorInvalidConfiguration;
+    const dim3 grid_dim((unsigned)((g.nP + 255) / 256), (unsigned)nb);
+    switch (ndim) {
+        case 1: k_sample_grid<1><<<grid_dim, 256, 0, s>>>(g, grid, C, data, out); break;
+        case 2: k_sample_grid<2><<<grid_dim, 256, 0, s>>>(g, grid, C, data, out); break;
+        default: k_sample_grid<3><<<grid_dim, 256, 0, s>>>(g, grid, C, data, out); break;
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_transform_data(const Tess &t, int nsteps, const float *lin, const int *outsize,

@@ -172,6 +172,9 @@ cudaError_t launch_ragged_points_backward(const Tess &t, int nsteps, int mode, i
                                           unsigned long long *ties, unsigned *err,
                                           cudaStream_t s);
 
+cudaError_t launch_sample_grid(int ndim, const float *grid, int nb, const float *data, int C,
+                               const int *size, const int *outsize, float *out, cudaStream_t s);
+
 int num_sms();
 
 }  // namespace cpab

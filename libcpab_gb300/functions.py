@@ -184,14 +184,13 @@ def transform_data(data, theta, params, outsize):
     return TransformData.apply(data, theta, params, outsize)
 
 
-def transform_data_from_host(data, theta, params, outsize, chunks=4, requires_grad=False):
+def transform_data_from_host(data, theta, params, outsize, requires_grad=False):
     """transform_data for a batch held in host memory: the batch is copied to
-    the GPU in `chunks` slices on a side stream and the fused forward of each
-    slice starts as soon as it has arrived (host_io.HostUpload), so the copy
-    overlaps with the integration.  Same result as
-    transform_data(data.cuda(), theta, params, outsize).  Returns (out, data
-    on the device); with requires_grad the device copy is a leaf whose .grad
-    receives d(data)."""
+    the GPU on a side stream (host_io.HostUpload) while the trajectories are
+    integrated, and sampled once it has arrived.  Same result as
+    transform_data(data.cuda(), theta, params, outsize), bit for bit.
+    Returns (out, data on the device); with requires_grad the device copy is
+    a leaf whose .grad receives d(data)."""
     from .host_io import HostUpload
     _require_cuda(theta)
     if data.is_cuda:
@@ -205,7 +204,7 @@ def transform_data_from_host(data, theta, params, outsize, chunks=4, requires_gr
     if params.numeric_grad or getattr(params, 'integration', 'fixed_step') == 'exact':
         dev = HostUpload(data, theta.device).wait().requires_grad_(requires_grad)
         return transform_data(dev, theta, params, outsize), dev
-    up = HostUpload(data, theta.device, chunks=chunks)
+    up = HostUpload(data, theta.device)
     dev = up.tensor.requires_grad_(requires_grad)
     return TransformData.apply(dev, theta, params, outsize, up), dev
 

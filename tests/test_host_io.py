@@ -28,8 +28,7 @@ def test_from_host_refuses_device_data():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize('gradient', ['reference', 'exact'])
-@pytest.mark.parametrize('chunks', [1, 3, 4, 16])
-def test_from_host_matches_device_path(cuda, gradient, chunks):
+def test_from_host_matches_device_path(cuda, gradient):
     import torch.nn.functional as F
     from libcpab_gb300 import Cpab
     from libcpab_gb300.host_io import HostUpload
@@ -41,8 +40,7 @@ def test_from_host_matches_device_path(cuda, gradient, chunks):
     data_h = torch.rand(nb, 3, 64, 48, generator=g).pin_memory()
     target_h = torch.rand(nb, 3, 64, 48, generator=g).pin_memory()
     th1 = theta_h.to(cuda).requires_grad_(True)
-    out1, dd1 = T.transform_data_from_host(data_h, th1, [64, 48], chunks=chunks,
-                                           requires_grad=True)
+    out1, dd1 = T.transform_data_from_host(data_h, th1, [64, 48], requires_grad=True)
     F.mse_loss(out1, HostUpload(target_h, cuda).wait()).backward()
     th2 = theta_h.to(cuda).requires_grad_(True)
     dd2 = data_h.to(cuda).requires_grad_(True)
@@ -54,3 +52,26 @@ def test_from_host_matches_device_path(cuda, gradient, chunks):
     # d(data) is a float-atomic scatter (summation order varies between runs)
     err = (dd1.grad - dd2.grad).abs().max() / dd2.grad.abs().max()
     assert float(err) <= 1e-5, float(err)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('nc,size,outsize', [([3, 3], [40, 30], [40, 30]),
+                                             ([2, 4], [31, 17], [20, 45]),
+                                             ([6], [50], [77]),
+                                             ([2, 2, 2], [9, 10, 11], [8, 12, 7])])
+def test_split_forward_is_bit_identical(cuda, nc, size, outsize):
+    """cpab_transform_grid_image + cpab_sample_grid == cpab_transform_data."""
+    from libcpab_gb300 import Cpab, _native as N
+    from libcpab_gb300.functions import basis_on
+    T = Cpab(nc, backend='pytorch', device='gpu', zero_boundary=True)
+    g = torch.Generator().manual_seed(1)
+    nb = 3
+    theta = torch.randn(nb, T.get_theta_dim(), generator=g).to(cuda)
+    data = torch.rand(nb, 2, *size, generator=g).to(cuda)
+    A, _, E = N.cell_tables(nc, 50, theta, basis_on(T.params, cuda))
+    lin = torch.cat([torch.linspace(0, 1, o, device=cuda) for o in outsize]).contiguous()
+    out, grid = N.transform_data(nc, 50, lin, outsize, E, data, save_grid=True)
+    grid2 = N.transform_grid_image(nc, 50, lin, outsize, E)
+    out2 = N.sample_grid(data, grid2, outsize)
+    assert torch.equal(grid, grid2)
+    assert torch.equal(out, out2)
