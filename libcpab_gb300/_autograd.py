@@ -152,8 +152,8 @@ class TransformData(torch.autograd.Function):
         data_c = data.detach().to(torch.float32).contiguous()
         theta_c = theta.detach().to(torch.float32).contiguous()
         dev = data.device
-        lin = torch.cat([torch.linspace(params.domain_min[i], params.domain_max[i], outsize[i],
-                                        device=dev) for i in range(params.ndim)]).contiguous()
+        from .functions import grid_axes
+        lin = grid_axes(params, outsize, dev)
         basis = _basis(params, dev)
         A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis)
         mode = _mode(params)

@@ -57,7 +57,7 @@ struct Tess {
     int band[3];      // 1 if (float)(nc*inc) > nc*inc: floats in [nc*inc, wlim) exist
     int band_any;     // band[0] | band[1] | band[2]
     int tier2;        // 2D second-tier tie decisions apply (square cells, see cell_2d_tier2)
-    int pow2;         // nc[0] and nc[1] are powers of two: p / inc == p * nc exactly
+    int pow2;         // every nc[j] (j < ndim, ndim >= 2) is a power of two: p / inc == p * nc
     float ncf[3];     // nc as float
 };
 
@@ -99,7 +99,8 @@ inline int tess_init(int ndim, const int *nc, Tess *t) {
     t->tier2 = ndim == 2 && t->inc[0] == t->inc[1];
     for (int j = 0; j < 2; ++j)
         t->tier2 &= (double)nextafterf(t->wlim[j], 0.f) <= (double)t->wlim[j] - 0.000000001;
-    t->pow2 = ndim == 2 && (t->nc[0] & (t->nc[0] - 1)) == 0 && (t->nc[1] & (t->nc[1] - 1)) == 0;
+    t->pow2 = ndim >= 2;
+    for (int j = 0; j < ndim; ++j) t->pow2 &= (t->nc[j] & (t->nc[j] - 1)) == 0;
     if (ndim == 3) {
         t->clamp3[0] = (float)((double)((float)nc[0] * t->inc[0]) - 1e-8);
         t->clamp3[1] = (float)((double)((float)nc[1] * t->inc[1]) - 1e-8);
@@ -476,9 +477,66 @@ CPAB_HD inline int cell_3d_fast(float p0, float p1, float p2, const Tess &t) {
     return -1;
 }
 
+// Second tier for 3D with power-of-two cell counts (Tess::pow2): inc is then
+// 2^-k, so the reference's sub-cell coordinates r/inc (cpab_ops.cpp:150-155)
+// equal r * nc exactly in double, and its tetrahedron tests
+// (cpab_ops.cpp:165-177) are evaluated with the same double operations in the
+// same order.  With cell_3d_fast's push, clamp and exact split (all float
+// operations of the reference) this reproduces the reference's decision for
+// every finite point without fmod or division.  Ties on the tetrahedron
+// planes are common on regular grids (3 % of a 128^3 meshgrid at [4,4,4]).
+static CPAB_HD __noinline__ int cell_3d_tier2(float p0, float p1, float p2, const Tess &t) {
+    if (!t.pow2) return -1;
+    if (!(fabsf(p0) <= 1e30f) || !(fabsf(p1) <= 1e30f) || !(fabsf(p2) <= 1e30f)) return -1;
+    if (!(p0 >= 0.f && p0 <= 1.f && p1 >= 0.f && p1 <= 1.f)) {
+        const float h = 0.5f;
+        p0 = CPAB_SUB_RN(p0, h); p1 = CPAB_SUB_RN(p1, h); p2 = CPAB_SUB_RN(p2, h);
+        const float a0 = fabsf(p0), a1 = fabsf(p1), a2 = fabsf(p2);
+        const float s0 = (a0 < a1 && a0 < a2) ? CPAB_MUL_RN(h, t.inc[0]) : 0.0f;
+        const float s1 = (a1 < a0 && a0 < a2) ? CPAB_MUL_RN(h, t.inc[1]) : 0.0f;
+        const float s2 = (a2 < a0 && a0 < a1) ? CPAB_MUL_RN(h, t.inc[2]) : 0.0f;
+        if (a0 > h) p0 = copysignf(CPAB_SUB_RN(h, s0), p0);
+        if (a1 > h) p1 = copysignf(CPAB_SUB_RN(h, s1), p1);
+        if (a2 > h) p2 = copysignf(CPAB_SUB_RN(h, s2), p2);
+        p0 = CPAB_ADD_RN(p0, h); p1 = CPAB_ADD_RN(p1, h); p2 = CPAB_ADD_RN(p2, h);
+    }
+    const float c0 = (p0 < t.clamp3[0]) ? p0 : t.clamp3[0];
+    const float c1 = (p1 < t.clamp3[1]) ? p1 : t.clamp3[1];
+    float c2 = (0.f < p2) ? p2 : 0.f;
+    c2 = (c2 < t.clamp3[2]) ? c2 : t.clamp3[2];
+    float f0, f1, f2, r0, r1, r2;
+    split_exact(c0, t.inc[0], t.rinc[0], f0, r0);
+    split_exact(c1, t.inc[1], t.rinc[1], f1, r1);
+    split_exact(c2, t.inc[2], t.rinc[2], f2, r2);
+    const int i = small_float_to_int(fminf(f0, t.ncf[0] - 1.f));
+    const int j = small_float_to_int(fminf(f1, t.ncf[1] - 1.f));
+    const int k = small_float_to_int(fminf(f2, t.ncf[2] - 1.f));
+    double x = (double)r0 * (double)t.nc[0], y = (double)r1 * (double)t.nc[1];
+    const double z = (double)r2 * (double)t.nc[2];
+    if (((i ^ j ^ k) & 1) != 0) {
+        const double tmp = x;
+        x = y;
+        y = 1 - tmp;
+    }
+    const int c = 5 * (i + j * t.nc[0] + k * t.nc[0] * t.nc[1]);
+    if (-x - y + z >= 0) return c + 1;
+    if (x + y + z - 2 >= 0) return c + 2;
+    if (-x + y - z >= 0) return c + 3;
+    if (x - y - z >= 0) return c + 4;
+    return c;
+}
+
+// FP32-side decision of both 3D tiers (-1: the FP64 replica must decide).
+CPAB_HD inline int cell_3d_fp32(float p0, float p1, float p2, const Tess &t) {
+    const int c = cell_3d_fast(p0, p1, p2, t);
+    return c >= 0 ? c : cell_3d_tier2(p0, p1, p2, t);
+}
+
 __device__ __forceinline__ int cell_3d(float p0, float p1, float p2, const Tess &t,
                                        unsigned long long *ties) {
-    const int c = cell_3d_fast(p0, p1, p2, t);
+    int c = cell_3d_fast(p0, p1, p2, t);
+    if (c >= 0) return c;
+    c = cell_3d_tier2(p0, p1, p2, t);
     if (c >= 0) return c;
     if (ties) atomicAdd(ties, 1ull);
     return cell_3d_exact(p0, p1, p2, t);

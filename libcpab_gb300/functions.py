@@ -129,6 +129,26 @@ def basis_on(params, device):
     return t
 
 
+def grid_axes(params, outsize, device):
+    """The meshgrid's per-axis coordinates (torch.linspace per axis, as
+    uniform_meshgrid builds them) concatenated, for the fused kernels; cached
+    per (device, outsize, domain) outside CUDA-graph capture (a tensor made
+    during capture only receives its values when the graph replays)."""
+    key = (str(device), tuple(int(o) for o in outsize), tuple(params.domain_min[:params.ndim]),
+           tuple(params.domain_max[:params.ndim]))
+    cache = params.__dict__.setdefault('_axes_cache', {})
+    t = cache.get(key)
+    if t is not None:
+        return t
+    t = torch.cat([torch.linspace(params.domain_min[i], params.domain_max[i], outsize[i],
+                                  device=device) for i in range(params.ndim)]).contiguous()
+    if not torch.cuda.is_current_stream_capturing():
+        if len(cache) >= 16:
+            cache.clear()
+        cache[key] = t
+    return t
+
+
 def _require_cuda(*tensors):
     for t in tensors:
         if not t.is_cuda:

@@ -34,8 +34,8 @@ class SequentialTransformData(torch.autograd.Function):
         dev = data.device
         data_c = data.detach().to(torch.float32).contiguous()
         last = params_list[-1]
-        lin = torch.cat([torch.linspace(last.domain_min[i], last.domain_max[i], outsize[i],
-                                        device=dev) for i in range(last.ndim)]).contiguous()
+        from .functions import grid_axes
+        lin = grid_axes(last, outsize, dev)
         As, Es = [], []
         for p, th in zip(params_list, thetas):
             A, _, E = N.cell_tables(p.nc, p.nstepsolver, th.detach().to(torch.float32).contiguous(),

@@ -32,7 +32,7 @@ int main(int argc, char **argv) {
             fast[i] = cpab::cell_2d_fp32(x, y, t);
             exact[i] = cpab::cell_2d_exact(x, y, t);
         } else {
-            fast[i] = cpab::cell_3d_fast(x, y, z, t);
+            fast[i] = cpab::cell_3d_fp32(x, y, z, t);
             exact[i] = cpab::cell_3d_exact(x, y, z, t);
         }
     }
