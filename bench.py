@@ -743,6 +743,26 @@ def run_cpu_baseline(steps, n_img):
         '%d of 64 images (%d points) per step, median of %d' % (n_img, pts, len(times))
 
 
+def run_cpu_numpy(n_img=1):
+    """The reference's numpy backend (FP64, libcpab/numpy/transformer.py:22-61),
+    restated in oracle/oracle.py, timed on its transform_grid of n_img images'
+    224^2 grids.  Forward only: that backend has no gradient."""
+    from oracle.oracle import numpy_transform_grid
+    from libcpab_gb300.tessellation import make_tessellation
+    B = make_tessellation(NC, True, False).B
+    theta = THETA_STD * torch.randn(BATCH, B.shape[1], generator=torch.Generator().manual_seed(0))
+    lin = np.linspace(0, 1, SIZE)
+    gx, gy = np.meshgrid(lin, lin, indexing='xy')
+    grid = np.stack([gx.reshape(-1), gy.reshape(-1)])
+    t0 = time.perf_counter()
+    numpy_transform_grid(B, theta[:n_img].numpy(), grid, NC, NSTEPS)
+    dt = time.perf_counter() - t0
+    pts = n_img * SIZE * SIZE
+    return {'value': pts / dt, 'unit': 'points/s', 'cores': 1, 'kind': 'port',
+            'sample': '%d of 64 theta x 224^2 grid points, transform_grid forward only (the '
+                      'numpy backend has no gradient), one run' % n_img}
+
+
 def main():
     args = parse()
     rank, world, _ = dist_env()
@@ -782,6 +802,7 @@ def main():
             v, cores, sample = run_cpu_baseline(1, args.cpu_sample_images)
             res['cpu_baseline'] = {'value': v, 'unit': 'points/s', 'cores': cores,
                                    'kind': 'port', 'sample': sample}
+            res['cpu_numpy_forward'] = run_cpu_numpy()
         print(json.dumps(res))
 
 
