@@ -126,21 +126,49 @@ __device__ __forceinline__ void load_grid_tile(const Geo &g, const float *gb, in
     }
 }
 
-template <int N>
+// Forward.  A block takes the same tile of kImagesPerBlock images in turn and
+// keeps the next image's grid tile in flight (registers) while it samples the
+// current one.  With the channel count known at compile time (CC = C, 1..4)
+// a thread issues the corner loads of all channels before the first lerp:
+// the gathers are latency-bound, and the extra loads in flight took the
+// 1024 x 3 x 224^2 case from 3.7 to 4.5 TB/s.  CC = 0: any C, channel by
+// channel.
+constexpr int kImagesPerBlock = 2;
+
+template <int N, int CC>
 __global__ void __launch_bounds__(256)
     k_interpolate_tiled(Geo g, TileGeo tg, const float *__restrict__ data, int C,
                         const float *__restrict__ grid, float *__restrict__ out, int nb) {
     __shared__ float sp[N][kTile][kTile + 1];
+    constexpr int RR = kTile / kRows;
     int a0, z0, mid;
     tile_coords<N>(g, tg, blockIdx.x, a0, z0, mid);
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int A = g.outsize[0], Z = g.outsize[N - 1];
-    for (int b = blockIdx.y; b < nb; b += gridDim.y) {
+    float nxt[RR][N];   // the next image's grid tile, as load_grid_tile would stage it
+    auto fetch = [&](int b) {
+        const float *gb = grid + (long long)b * N * g.nP;
+#pragma unroll
+        for (int r = 0; r < RR; ++r) {
+            const int zl = ty + kRows * r, a = a0 + tx, z = z0 + zl;
+            const bool in = a < A && z < Z;
+            const int k = in ? grid_index<N>(g, a, mid, z) : 0;
+#pragma unroll
+            for (int j = 0; j < N; ++j) nxt[r][j] = in ? __ldg(gb + (long long)j * g.nP + k) : 0.f;
+        }
+    };
+    int b = blockIdx.y;
+    if (b < nb) fetch(b);
+    for (; b < nb; b += gridDim.y) {
         __syncthreads();
-        load_grid_tile<N>(g, grid + (long long)b * N * g.nP, a0, z0, mid, sp);
+#pragma unroll
+        for (int r = 0; r < RR; ++r)
+#pragma unroll
+            for (int j = 0; j < N; ++j) sp[j][ty + kRows * r][tx] = nxt[r][j];
         __syncthreads();
+        if (b + (int)gridDim.y < nb) fetch(b + gridDim.y);
 #pragma unroll 1
-        for (int r = 0; r < kTile / kRows; ++r) {
+        for (int r = 0; r < RR; ++r) {
             const int al = ty + kRows * r, a = a0 + al, z = z0 + tx;
             if (a >= A || z >= Z) continue;
             float p[N];
@@ -148,9 +176,22 @@ __global__ void __launch_bounds__(256)
             for (int j = 0; j < N; ++j) p[j] = sp[j][tx][al];
             const Corner<N> cr = corners<N>(p, g);
             const int o = out_index<N>(g, a, mid, z);
-            for (int c = 0; c < C; ++c) {
-                const long long plane = (long long)b * C + c;
-                out[plane * g.nP + o] = lerp_corners<N>(data + plane * g.nD, cr);
+            if constexpr (CC > 0) {
+                float v[CC][1 << N];
+#pragma unroll
+                for (int c = 0; c < CC; ++c) {
+                    const float *D = data + ((long long)b * CC + c) * g.nD;
+#pragma unroll
+                    for (int m = 0; m < (1 << N); ++m) v[c][m] = __ldg(D + cr.off[m]);
+                }
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+                    out[((long long)b * CC + c) * g.nP + o] = lerp_values<N>(v[c], cr.f);
+            } else {
+                for (int c = 0; c < C; ++c) {
+                    const long long plane = (long long)b * C + c;
+                    out[plane * g.nP + o] = lerp_corners<N>(data + plane * g.nD, cr);
+                }
             }
         }
     }
@@ -233,9 +274,26 @@ cudaError_t launch_interpolate(int ndim, const float *data, int nb, int C, const
     }
     unsigned blocks = 0;
     const TileGeo tg = make_tiles(ndim, g, &blocks);
-    const dim3 tgrid(blocks, gridn.y);
-    if (ndim == 2) k_interpolate_tiled<2><<<tgrid, block, 0, s>>>(g, tg, data, C, grid, out, nb);
-    else k_interpolate_tiled<3><<<tgrid, block, 0, s>>>(g, tg, data, C, grid, out, nb);
+    const dim3 tgrid(blocks, (gridn.y + kImagesPerBlock - 1) / kImagesPerBlock);
+#define CPAB_IT(NN, CC) k_interpolate_tiled<NN, CC><<<tgrid, block, 0, s>>>(g, tg, data, C, grid, out, nb)
+    if (ndim == 2) {
+        switch (C) {
+            case 1: CPAB_IT(2, 1); break;
+            case 2: CPAB_IT(2, 2); break;
+            case 3: CPAB_IT(2, 3); break;
+            case 4: CPAB_IT(2, 4); break;
+            default: CPAB_IT(2, 0); break;
+        }
+    } else {
+        switch (C) {
+            case 1: CPAB_IT(3, 1); break;
+            case 2: CPAB_IT(3, 2); break;
+            case 3: CPAB_IT(3, 3); break;
+            case 4: CPAB_IT(3, 4); break;
+            default: CPAB_IT(3, 0); break;
+        }
+    }
+#undef CPAB_IT
     return cudaGetLastError();
 }
 
