@@ -167,6 +167,7 @@ class TransformData(torch.autograd.Function):
                 raise ValueError('data must be the uploaded tensor')
             grid = N.transform_grid_image(params.nc, params.nstepsolver, lin, outsize, E,
                                           ties=_ties(params))
+            upload.start()   # the integration is already queued
             upload.wait()
             out = N.sample_grid(data_c, grid, outsize)
             if not save_grid:

@@ -318,18 +318,19 @@ __device__ __forceinline__ void logged_forward(const AdjSmem<N, CT> &sm, const T
                                                int nsteps, const Steps &st, float (&p)[N],
                                                unsigned long long *ties, unsigned *err) {
     const int B = blockDim.x, tid = threadIdx.x;
-    for (int n = 0; n < nsteps; ++n) {
-        if (n % kSeg == 0) {
+    for (int n0 = 0, seg = 0; n0 < nsteps; n0 += kSeg, ++seg) {
 #pragma unroll
-            for (int r = 0; r < N; ++r) sm.ck[((n / kSeg) * N + r) * B + tid] = p[r];
+        for (int r = 0; r < N; ++r) sm.ck[(seg * N + r) * B + tid] = p[r];
+        const int end = min(n0 + kSeg, nsteps);
+        for (int n = n0; n < end; ++n) {
+            int c = find_cell<N>(p, t, ties);
+            if ((unsigned)c >= (unsigned)t.nC) {
+                raise_error(err, kErrBadCell);
+                c = 0;
+            }
+            sm.cl[n * B + tid] = (CT)c;
+            traj_step<N, MODE>(sm.tab, c, st, p);
         }
-        int c = find_cell<N>(p, t, ties);
-        if ((unsigned)c >= (unsigned)t.nC) {
-            raise_error(err, kErrBadCell);
-            c = 0;
-        }
-        sm.cl[n * B + tid] = (CT)c;
-        traj_step<N, MODE>(sm.tab, c, st, p);
     }
 }
 

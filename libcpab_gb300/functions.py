@@ -224,7 +224,7 @@ def transform_data_from_host(data, theta, params, outsize, requires_grad=False):
     if params.numeric_grad or getattr(params, 'integration', 'fixed_step') == 'exact':
         dev = HostUpload(data, theta.device).wait().requires_grad_(requires_grad)
         return transform_data(dev, theta, params, outsize), dev
-    up = HostUpload(data, theta.device)
+    up = HostUpload(data, theta.device, start=False)   # copied once the integration is queued
     dev = up.tensor.requires_grad_(requires_grad)
     return TransformData.apply(dev, theta, params, outsize, up), dev
 

@@ -46,9 +46,13 @@ class HostUpload:
     """Copy a host tensor to `device` in `chunks` slices of its first axis on
     the copy stream.  `tensor` is the device tensor (usable once the matching
     event has been waited for); wait(k) makes the current stream wait for
-    chunk k, wait() for all of them, and returns the tensor."""
+    chunk k, wait() for all of them, and returns the tensor.  With
+    start=False only the device tensor is allocated; start() (or the first
+    wait()) enqueues the copies, so a caller can launch work that does not
+    need the data first."""
 
-    def __init__(self, host: torch.Tensor, device, chunks: int = 1, dtype=torch.float32):
+    def __init__(self, host: torch.Tensor, device, chunks: int = 1, dtype=torch.float32,
+                 start: bool = True):
         if host.is_cuda:
             raise ValueError('HostUpload takes a host tensor')
         device = torch.device(device)
@@ -61,15 +65,29 @@ class HostUpload:
             host = host.pin_memory()
         self.host = host
         cur = torch.cuda.current_stream(device)
-        cs = copy_stream(device)
+        self._cs = copy_stream(device)
         n = host.shape[0] if host.dim() > 0 else 1
         self.bounds = chunk_bounds(n, chunks) if host.dim() > 0 else [(0, 1)]
         self.events = []
-        with torch.cuda.stream(cs):
+        with torch.cuda.stream(self._cs):
             # allocated on the copy stream: the allocator hands it a block
-            # whose earlier users are ordered before this copy, so the copy
+            # whose earlier users are ordered before the copy, so the copy
             # need not wait for the current stream's queued kernels
             self.tensor = torch.empty(host.shape, dtype=dtype, device=device)
+        # consumers run on the current stream: the block is reused only after
+        # their queued work is done
+        self.tensor.record_stream(cur)
+        self.started = False
+        if start:
+            self.start()
+
+    def start(self):
+        """Enqueue the copies (once)."""
+        if self.started:
+            return
+        self.started = True
+        host, cs = self.host, self._cs
+        with torch.cuda.stream(cs):
             for a, b in self.bounds:
                 if host.dim() > 0:
                     self.tensor[a:b].copy_(host[a:b], non_blocking=True)
@@ -78,11 +96,9 @@ class HostUpload:
                 ev = torch.cuda.Event()
                 ev.record(cs)
                 self.events.append(ev)
-        # consumers run on the current stream: the block is reused only after
-        # their queued work is done
-        self.tensor.record_stream(cur)
 
     def wait(self, k: int | None = None) -> torch.Tensor:
+        self.start()
         cur = torch.cuda.current_stream(self.tensor.device)
         for ev in (self.events if k is None else [self.events[k]]):
             cur.wait_event(ev)
