@@ -243,6 +243,50 @@ __device__ __forceinline__ void warp_flush(bool flush, int cell, const float (&a
     }
 }
 
+// 1D variant of warp_flush.  A 1D flow keeps the order of points, so the
+// lanes of a warp holding consecutive points of a sorted grid (the ragged
+// series) sit in non-decreasing cells: equal cells form contiguous lane runs.
+// Then every lane takes part in a fixed five-round shuffle tree over its run
+// (non-flushing lanes add zeros) and the run's lowest lane adds the sum if
+// any lane of the run flushes: the same one-add-per-element-per-step
+// discipline as flush_cells, without match.any.  Unsorted warps use
+// warp_flush.  Called by all lanes of the warp.
+template <int P>
+__device__ __forceinline__ void warp_flush_1d(bool flush, int cell, const float (&acc)[P],
+                                              float *warp_tab) {
+    const unsigned fm = __ballot_sync(0xffffffffu, flush);
+    if (!fm) return;
+    const int lane = threadIdx.x & 31;
+    const int prev = __shfl_up_sync(0xffffffffu, cell, 1);
+    if (__any_sync(0xffffffffu, lane > 0 && prev > cell)) {
+        warp_flush<P>(flush, cell, acc, warp_tab);
+        return;
+    }
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != cell);
+    const unsigned le = 0xffffffffu >> (31 - lane);            // lanes <= lane
+    const int lo = 31 - __clz(heads & le);
+    const unsigned above = heads & ~le;
+    const int hi = above ? __ffs(above) - 2 : 31;
+    float sum[P];
+#pragma unroll
+    for (int i = 0; i < P; ++i) sum[i] = flush ? acc[i] : 0.f;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+            const float u = __shfl_down_sync(0xffffffffu, sum[i], off);
+            if (lane + off <= hi) sum[i] += u;
+        }
+    }
+    const unsigned run = (hi == 31 ? 0xffffffffu : ((1u << (hi + 1)) - 1u)) & ~((1u << lo) - 1u);
+    if (lane == lo && (fm & run)) {
+        float *dst = warp_tab + cell * P;
+#pragma unroll
+        for (int i = 0; i < P; ++i) dst[i] += sum[i];
+    }
+    __syncwarp();
+}
+
 // Reverse sweep of one trajectory whose cells are logged in cl and whose
 // checkpoints are in ck; lam holds dL/dp_N on entry and dL/dp_0 on exit.
 // Each segment's positions are rebuilt from its checkpoint with the logged
@@ -276,7 +320,8 @@ __device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nste
         for (int s = len - 1; s >= 0; --s) {
             const int c = (int)sm.cl[(n0 + s) * B + tid];
             const bool change = c != gcell;
-            warp_flush<P>(change && gcell >= 0 && live, gcell, acc, warp_tab);
+            if constexpr (N == 1) warp_flush_1d<P>(change && gcell >= 0 && live, gcell, acc, warp_tab);
+            else warp_flush<P>(change && gcell >= 0 && live, gcell, acc, warp_tab);
             if (change) {
                 gcell = c;
 #pragma unroll
@@ -288,7 +333,8 @@ __device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nste
             adjoint_step<N>(sm.dtab, c, p, lam, acc);
         }
     }
-    warp_flush<P>(gcell >= 0 && live, gcell, acc, warp_tab);
+    if constexpr (N == 1) warp_flush_1d<P>(gcell >= 0 && live, gcell, acc, warp_tab);
+    else warp_flush<P>(gcell >= 0 && live, gcell, acc, warp_tab);
 }
 
 // Sweep with the arithmetic of k_integrate's compensated path,
