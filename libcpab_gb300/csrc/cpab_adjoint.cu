@@ -46,19 +46,22 @@
 
 namespace cpab {
 
-template <int N, int MODE, typename CT>
+template <int N, int MODE, typename CT, bool GWG>
 __global__ void __launch_bounds__(256)
     k_adjoint(Tess t, int nsteps, Steps st, const float *__restrict__ points, int broadcast,
               long long nP, const float *__restrict__ table, int parts, int tiles,
               const float *__restrict__ gout, float *__restrict__ dpoints,
-              float *__restrict__ partials, unsigned long long *ties, unsigned *err) {
+              float *__restrict__ partials, float *gw_ext, unsigned long long *ties,
+              unsigned *err) {
     extern __shared__ float4 smem4[];
     __shared__ uint64_t bar;
     const int B = blockDim.x, tid = threadIdx.x;
     const int G = t.nC * N * (N + 1);
-    const AdjSmem<N, CT> sm = carve_adjoint<N, CT>(reinterpret_cast<float *>(smem4), t.nC, nsteps);
-
     const int th = blockIdx.y, part = blockIdx.x;
+    float *gw = GWG ? gw_ext + ((size_t)th * parts + part) * (B / 32) * round4(G) : nullptr;
+    const AdjSmem<N, CT> sm =
+        carve_adjoint<N, CT, GWG>(reinterpret_cast<float *>(smem4), t.nC, nsteps, gw);
+
     if (!adjoint_prologue<N, MODE, CT>(sm, table + (long long)th * G, t.nC, st, &bar, err)) return;
     float *warp_tab = sm.gw + (size_t)(tid >> 5) * round4(G);
     const float *src = points + (broadcast ? (long long)th * N * nP : 0ll);
@@ -83,47 +86,42 @@ __global__ void __launch_bounds__(256)
 
 // ------------------------------ planning -------------------------------------
 template <int N, int MODE, typename CT>
-static bool plan_t(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan) {
-    int dev = 0, max_optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (max_optin <= 0) max_optin = 48 * 1024;
-    const int cands[3] = {256, 128, 64};
-    for (int ci = 0; ci < 3; ++ci) {
-        const int block = cands[ci];
-        const size_t smem = adjoint_smem_bytes<N, CT>(t.nC, nsteps, block) + 64;
-        if (smem > (size_t)max_optin) continue;
-        auto kern = k_adjoint<N, MODE, CT>;
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-            return false;
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
-        if (per_sm <= 0) continue;
-        const long long tiles = (nP + block - 1) / block;
-        const long long target = 2ll * num_sms() * per_sm;
-        long long parts = (target + n_theta - 1) / n_theta;
-        if (parts > tiles) parts = tiles;
-        if (parts < 1) parts = 1;
-        plan->block = block;
-        plan->tiles = (int)tiles;
-        plan->parts = (int)parts;
-        plan->smem = smem;
-        plan->partial_floats = (size_t)n_theta * parts * t.nC * N * (N + 1);
-        return true;
-    }
-    return false;
+static bool plan_t(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan,
+                   bool allow_global) {
+    int block = 0, per_sm = 0;
+    bool global_gw = false;
+    size_t smem = 0;
+    // global per-warp tables only in 3D, where the tables are large
+    decltype(&k_adjoint<N, MODE, CT, false>) kg = nullptr;
+    if constexpr (N == 3)
+        if (allow_global) kg = k_adjoint<N, MODE, CT, true>;
+    if (!adjoint_shape<N, CT>(k_adjoint<N, MODE, CT, false>, kg, t.nC, nsteps, &block,
+                              &global_gw, &smem, &per_sm))
+        return false;
+    const long long tiles = (nP + block - 1) / block;
+    const long long target = 2ll * num_sms() * per_sm;
+    long long parts = (target + n_theta - 1) / n_theta;
+    if (parts > tiles) parts = tiles;
+    if (parts < 1) parts = 1;
+    plan->block = block;
+    plan->tiles = (int)tiles;
+    plan->parts = (int)parts;
+    plan->smem = smem;
+    plan->partial_floats = (size_t)n_theta * parts * t.nC * N * (N + 1);
+    plan->gw_floats = global_gw ? (size_t)n_theta * parts * (block / 32) * round4(t.nC * N * (N + 1))
+                                : 0;
+    return true;
 }
 
 bool plan_adjoint_mode(const Tess &t, int nsteps, int mode, long long nP, int n_theta,
-                       AdjointPlan *plan) {
+                       AdjointPlan *plan, bool allow_global) {
     const bool small = t.nC <= 256;
 #define CPAB_PLAN(N)                                                                          \
     if (mode == 0)                                                                            \
-        return small ? plan_t<N, 0, uint8_t>(t, nsteps, nP, n_theta, plan)                    \
-                     : plan_t<N, 0, uint16_t>(t, nsteps, nP, n_theta, plan);                  \
-    return small ? plan_t<N, 1, uint8_t>(t, nsteps, nP, n_theta, plan)                        \
-                 : plan_t<N, 1, uint16_t>(t, nsteps, nP, n_theta, plan);
+        return small ? plan_t<N, 0, uint8_t>(t, nsteps, nP, n_theta, plan, allow_global)      \
+                     : plan_t<N, 0, uint16_t>(t, nsteps, nP, n_theta, plan, allow_global);    \
+    return small ? plan_t<N, 1, uint8_t>(t, nsteps, nP, n_theta, plan, allow_global)          \
+                 : plan_t<N, 1, uint16_t>(t, nsteps, nP, n_theta, plan, allow_global);
     switch (t.ndim) {
         case 1: { CPAB_PLAN(1) }
         case 2: { CPAB_PLAN(2) }
@@ -132,10 +130,11 @@ bool plan_adjoint_mode(const Tess &t, int nsteps, int mode, long long nP, int n_
 #undef CPAB_PLAN
 }
 
-bool plan_adjoint(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan) {
+bool plan_adjoint(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan,
+                  bool allow_global) {
     // Both modes share the shared-memory layout; plan with the larger register
     // footprint (mode 0) so the plan is valid for either.
-    return plan_adjoint_mode(t, nsteps, 0, nP, n_theta, plan);
+    return plan_adjoint_mode(t, nsteps, 0, nP, n_theta, plan, allow_global);
 }
 
 template <int N, int MODE, typename CT>
@@ -144,7 +143,9 @@ static cudaError_t launch_adjoint_t(const Tess &t, int nsteps, const AdjointPlan
                                     const float *table, int n_theta, const float *gout,
                                     float *dpoints, float *partials, unsigned long long *ties,
                                     unsigned *err, cudaStream_t s) {
-    auto kern = k_adjoint<N, MODE, CT>;
+    auto kern = k_adjoint<N, MODE, CT, false>;
+    if constexpr (N == 3)
+        if (plan.gw_floats) kern = k_adjoint<N, MODE, CT, true>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)plan.smem);
     if (e != cudaSuccess) return e;
@@ -152,9 +153,10 @@ static cudaError_t launch_adjoint_t(const Tess &t, int nsteps, const AdjointPlan
     if (n_theta == 0) return cudaSuccess;
     if (n_theta > 65535) return cudaErrorInvalidConfiguration;   // theta on grid y
     const dim3 grid((unsigned)plan.parts, (unsigned)n_theta);
+    float *gw = plan.gw_floats ? partials + plan.gw_offset() : nullptr;
     kern<<<grid, plan.block, plan.smem, s>>>(t, nsteps, st, points, broadcast, nP, table,
                                                        plan.parts, plan.tiles, gout, dpoints,
-                                                       partials, ties, err);
+                                                       partials, gw, ties, err);
     return cudaGetLastError();
 }
 

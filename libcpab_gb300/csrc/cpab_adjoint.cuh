@@ -123,23 +123,62 @@ __host__ __device__ inline int round4(int x) { return (x + 3) & ~3; }
 // Shared memory carve-up for the adjoint kernels (floats unless noted):
 //   tab   [round4(G)]            cell table of this theta (TMA destination)
 //   dtab  [round4(nC*stride)]    per-cell adjoint propagators D
-//   gw    [W][round4(G)]         per-warp cell-gradient tables
+//   gw    [W][round4(G)]         per-warp cell-gradient tables (or in global memory, see
+//                                carve_adjoint)
 //   ck    [nseg][N][block]       checkpoints (position every kSeg steps)
 //   pb    [kSeg][N][block]       positions of the segment being reversed
 //   cl    [nsteps][block] (CT)   per-step cells
 // Per-thread arrays are indexed [...][block] by thread, so warps access
 // consecutive words (no bank conflicts).
 template <int N, typename CT>
-__host__ __device__ inline size_t adjoint_smem_bytes(int nC, int nsteps, int block) {
+__host__ __device__ inline size_t adjoint_smem_bytes(int nC, int nsteps, int block,
+                                                     bool gw_in_smem = true) {
     constexpr int P = N * (N + 1);
     const int G = round4(nC * P);
     const int Dn = round4(nC * dtab_stride<N>());
-    const int W = block / 32;
+    const int W = gw_in_smem ? block / 32 : 0;
     const int nseg = (nsteps + kSeg - 1) / kSeg;
     size_t b = (size_t)G * 4 + (size_t)Dn * 4 + (size_t)W * G * 4 +
                (size_t)nseg * N * block * 4 + (size_t)kSeg * N * block * 4 +
                (size_t)nsteps * block * sizeof(CT);
     return (b + 15) & ~(size_t)15;
+}
+
+// Host: the launch shape of an adjoint kernel with the most resident warps per
+// SM among 256/128/64 threads per CTA and per-warp tables in shared memory
+// (kern_shared) or in global memory (kern_global, may be nullptr; see
+// carve_adjoint).  Ties keep shared memory and the larger CTA.
+template <int N, typename CT, typename K>
+inline bool adjoint_shape(K kern_shared, K kern_global, int nC, int nsteps, int *block,
+                          bool *global_gw, size_t *smem, int *per_sm) {
+    const bool allow_global = kern_global != nullptr;
+    int dev = 0, max_optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (max_optin <= 0) max_optin = 48 * 1024;
+    const int cands[3] = {256, 128, 64};
+    int best = 0;
+    for (int g = 0; g < (allow_global ? 2 : 1); ++g) {
+        for (int ci = 0; ci < 3; ++ci) {
+            const int b = cands[ci];
+            const size_t sm = adjoint_smem_bytes<N, CT>(nC, nsteps, b, g == 0) + 64;
+            if (sm > (size_t)max_optin) continue;
+            const K kern = g == 0 ? kern_shared : kern_global;
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sm) != cudaSuccess)
+                return false;
+            int n = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, b, sm);
+            if (n * (b / 32) > best) {
+                best = n * (b / 32);
+                *block = b;
+                *global_gw = g == 1;
+                *smem = sm;
+                *per_sm = n;
+            }
+        }
+    }
+    return best > 0;
 }
 
 template <int N, typename CT>
@@ -148,8 +187,13 @@ struct AdjSmem {
     CT *cl;
 };
 
-template <int N, typename CT>
-__device__ __forceinline__ AdjSmem<N, CT> carve_adjoint(float *base, int nC, int nsteps) {
+// GWG: gw_ext is this CTA's W per-warp tables in global memory (L2-resident;
+// each warp owns its table, so the flush stays a plain read-add-write), else
+// the tables are in shared memory.  Global tables free shared memory for more
+// resident warps when the tables are large (3D, hundreds of cells).
+template <int N, typename CT, bool GWG = false>
+__device__ __forceinline__ AdjSmem<N, CT> carve_adjoint(float *base, int nC, int nsteps,
+                                                        float *gw_ext = nullptr) {
     constexpr int P = N * (N + 1);
     const int B = blockDim.x, W = B / 32;
     const int Gr = round4(nC * P);
@@ -157,8 +201,14 @@ __device__ __forceinline__ AdjSmem<N, CT> carve_adjoint(float *base, int nC, int
     AdjSmem<N, CT> s;
     s.tab = base;
     s.dtab = s.tab + Gr;
-    s.gw = s.dtab + round4(nC * dtab_stride<N>());
-    s.ck = s.gw + (size_t)W * Gr;
+    float *after = s.dtab + round4(nC * dtab_stride<N>());
+    if constexpr (GWG) {   // a template choice keeps the shared-memory path's
+        s.gw = gw_ext;     // flushes on shared-memory instructions
+        s.ck = after;
+    } else {
+        s.gw = after;
+        s.ck = after + (size_t)W * Gr;
+    }
     s.pb = s.ck + (size_t)nseg * N * B;
     s.cl = reinterpret_cast<CT *>(s.pb + (size_t)kSeg * N * B);
     return s;

@@ -190,7 +190,7 @@ size_t cpab_backward_workspace(int ndim, const int *nc, int nsteps, long long nP
         fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
         return 0;
     }
-    return plan.partial_floats * sizeof(float);
+    return plan.ws_floats() * sizeof(float);
 }
 
 int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *points,
@@ -220,7 +220,7 @@ int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *po
     AdjointPlan plan;
     if (!plan_adjoint(t, nsteps, nP, n_theta, &plan))
         return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
-    const size_t need = plan.partial_floats * sizeof(float);
+    const size_t need = plan.ws_floats() * sizeof(float);
     if (!workspace || workspace_bytes < need)
         return fail(CPAB_ERR_WORKSPACE, "workspace of %zu bytes needed (got %zu)", need,
                     workspace ? workspace_bytes : (size_t)0);
@@ -337,7 +337,7 @@ size_t cpab_transform_data_backward_workspace(int ndim, const int *nc, int nstep
         fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
         return 0;
     }
-    return plan.partial_floats * sizeof(float);
+    return plan.ws_floats() * sizeof(float);
 }
 
 }  // extern "C"
@@ -371,7 +371,7 @@ static int td_backward(int ndim, const int *nc, int nsteps, int mode, const floa
     AdjointPlan plan;
     if (!plan_transform_data_backward(t, nsteps, mode, nP, nb, &plan))
         return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
-    const size_t need = plan.partial_floats * sizeof(float);
+    const size_t need = plan.ws_floats() * sizeof(float);
     if (!workspace || workspace_bytes < need)
         return fail(CPAB_ERR_WORKSPACE, "workspace of %zu bytes needed (got %zu)", need,
                     workspace ? workspace_bytes : (size_t)0);
@@ -912,8 +912,8 @@ int cpab_backward_noalloc(int ndim, const int *nc, int nsteps, int mode, const f
                     "no-alloc scratch holds %zu floats; this problem needs at least %zu "
                     "(n_theta * nC * ndim * (ndim+1)); use cpab_backward with a workspace",
                     kNoAllocScratchFloats, slice);
-    AdjointPlan plan;
-    if (!plan_adjoint(t, nsteps, nP, n_theta, &plan))
+    AdjointPlan plan;   // per-warp tables in shared memory: the scratch holds the partials only
+    if (!plan_adjoint(t, nsteps, nP, n_theta, &plan, false))
         return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
     const long long fit = (long long)(kNoAllocScratchFloats / slice);
     if (plan.parts > fit) plan.parts = (int)fit;

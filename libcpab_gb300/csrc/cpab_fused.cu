@@ -164,21 +164,24 @@ cudaError_t launch_transform_data(const Tess &t, int nsteps, const float *lin, c
 #undef CPAB_TD
 }
 
-template <int N, int MODE, typename CT>
+template <int N, int MODE, typename CT, bool GWG>
 __global__ void __launch_bounds__(256)
     k_transform_data_backward(Tess t, int nsteps, Steps st, Geo g, PreStages pre,
                               const float *__restrict__ lin, const float *__restrict__ table,
                               const float *__restrict__ grid_saved, int C,
                               const float *__restrict__ data, const float *__restrict__ gout,
-                              float *__restrict__ ddata, float *__restrict__ partials, int parts,
-                              int tiles, unsigned long long *ties, unsigned *err) {
+                              float *__restrict__ ddata, float *__restrict__ partials,
+                              float *gw_ext, int parts, int tiles, unsigned long long *ties,
+                              unsigned *err) {
     extern __shared__ float4 smem4[];
     __shared__ uint64_t bar;
     const int B = blockDim.x, tid = threadIdx.x;
     const int G = t.nC * N * (N + 1);
-    const AdjSmem<N, CT> sm = carve_adjoint<N, CT>(reinterpret_cast<float *>(smem4), t.nC, nsteps);
-
     const int b = blockIdx.y, part = blockIdx.x;
+    float *gw = GWG ? gw_ext + ((size_t)b * parts + part) * (B / 32) * round4(G) : nullptr;
+    const AdjSmem<N, CT> sm =
+        carve_adjoint<N, CT, GWG>(reinterpret_cast<float *>(smem4), t.nC, nsteps, gw);
+
     if (!adjoint_prologue<N, MODE, CT>(sm, table + (long long)b * G, t.nC, st, &bar, err)) return;
     float *warp_tab = sm.gw + (size_t)(tid >> 5) * round4(G);
 
@@ -225,35 +228,28 @@ __global__ void __launch_bounds__(256)
 
 template <int N, int MODE, typename CT>
 static bool plan_td_t(const Tess &t, int nsteps, long long nP, int nb, AdjointPlan *plan) {
-    int dev = 0, max_optin = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (max_optin <= 0) max_optin = 48 * 1024;
-    const int cands[3] = {256, 128, 64};
-    for (int ci = 0; ci < 3; ++ci) {
-        const int block = cands[ci];
-        const size_t smem = adjoint_smem_bytes<N, CT>(t.nC, nsteps, block) + 64;
-        if (smem > (size_t)max_optin) continue;
-        auto kern = k_transform_data_backward<N, MODE, CT>;
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-            return false;
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
-        if (per_sm <= 0) continue;
-        const long long tiles = (nP + block - 1) / block;
-        const long long target = 2ll * num_sms() * per_sm;
-        long long parts = (target + nb - 1) / nb;
-        if (parts > tiles) parts = tiles;
-        if (parts < 1) parts = 1;
-        plan->block = block;
-        plan->tiles = (int)tiles;
-        plan->parts = (int)parts;
-        plan->smem = smem;
-        plan->partial_floats = (size_t)nb * parts * t.nC * N * (N + 1);
-        return true;
-    }
-    return false;
+    int block = 0, per_sm = 0;
+    bool global_gw = false;
+    size_t smem = 0;
+    // global per-warp tables only in 3D, where the tables are large
+    decltype(&k_transform_data_backward<N, MODE, CT, false>) kg = nullptr;
+    if constexpr (N == 3) kg = k_transform_data_backward<N, MODE, CT, true>;
+    if (!adjoint_shape<N, CT>(k_transform_data_backward<N, MODE, CT, false>, kg, t.nC, nsteps,
+                              &block, &global_gw, &smem, &per_sm))
+        return false;
+    const long long tiles = (nP + block - 1) / block;
+    const long long target = 2ll * num_sms() * per_sm;
+    long long parts = (target + nb - 1) / nb;
+    if (parts > tiles) parts = tiles;
+    if (parts < 1) parts = 1;
+    plan->block = block;
+    plan->tiles = (int)tiles;
+    plan->parts = (int)parts;
+    plan->smem = smem;
+    plan->partial_floats = (size_t)nb * parts * t.nC * N * (N + 1);
+    plan->gw_floats = global_gw ? (size_t)nb * parts * (block / 32) * round4(t.nC * N * (N + 1))
+                                : 0;
+    return true;
 }
 
 bool plan_transform_data_backward(const Tess &t, int nsteps, int mode, long long nP, int nb,
@@ -280,7 +276,9 @@ static cudaError_t launch_td_bwd_t(const Tess &t, int nsteps, const AdjointPlan 
                                    const float *grid_saved, int nb, const float *data, int C,
                                    const float *gout, float *ddata, float *partials,
                                    unsigned long long *ties, unsigned *err, cudaStream_t s) {
-    auto kern = k_transform_data_backward<N, MODE, CT>;
+    auto kern = k_transform_data_backward<N, MODE, CT, false>;
+    if constexpr (N == 3)
+        if (plan.gw_floats) kern = k_transform_data_backward<N, MODE, CT, true>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)plan.smem);
     if (e != cudaSuccess) return e;
@@ -288,8 +286,9 @@ static cudaError_t launch_td_bwd_t(const Tess &t, int nsteps, const AdjointPlan 
     if (nb == 0) return cudaSuccess;
     if (nb > 65535) return cudaErrorInvalidConfiguration;   // images on grid y
     const dim3 grid((unsigned)plan.parts, (unsigned)nb);
+    float *gw = plan.gw_floats ? partials + plan.gw_offset() : nullptr;
     kern<<<grid, plan.block, plan.smem, s>>>(t, nsteps, st, g, pre, lin, table, grid_saved, C,
-                                                       data, gout, ddata, partials, plan.parts,
+                                                       data, gout, ddata, partials, gw, plan.parts,
                                                        plan.tiles, ties, err);
     return cudaGetLastError();
 }

@@ -39,10 +39,16 @@ struct AdjointPlan {
     int tiles;           // point tiles per theta
     size_t smem;         // dynamic shared memory bytes
     size_t partial_floats;
+    size_t gw_floats;    // per-warp cell tables in the workspace (0: in shared memory)
+    // workspace layout: partials [partial_floats], then (64-float aligned) the
+    // per-warp tables [n_theta][parts][warps][round4(G)]
+    size_t gw_offset() const { return (partial_floats + 63) & ~(size_t)63; }
+    size_t ws_floats() const { return gw_floats ? gw_offset() + gw_floats : partial_floats; }
 };
-bool plan_adjoint(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan);
+bool plan_adjoint(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan,
+                  bool allow_global_gw = true);
 bool plan_adjoint_mode(const Tess &t, int nsteps, int mode, long long nP, int n_theta,
-                       AdjointPlan *plan);
+                       AdjointPlan *plan, bool allow_global_gw = true);
 cudaError_t launch_adjoint(const Tess &t, int nsteps, int mode, const AdjointPlan &plan,
                            const float *points, int broadcast, long long nP, const float *table,
                            int n_theta, const float *gout, float *dpoints, float *partials,
