@@ -93,6 +93,31 @@ def test_noalloc_3d_and_large_batch(cuda):
         assert _rel(dth, ref_dth) <= 1e-5
 
 
+@pytest.mark.parametrize('mode', [0, 1])
+def test_3d_global_warp_tables_match_shared(mode, cuda):
+    """3D [4,4,4] (320 cells): cpab_backward keeps its per-warp gradient tables
+    in the workspace (more warps per SM); the no-alloc entry point keeps them
+    in shared memory.  Same dpoints bit for bit, dtheta to summation order."""
+    from libcpab_gb300 import _native as N
+    from libcpab_gb300.tessellation import make_tessellation
+    g = load_golden('L_3d_4x4x4_zb_vp')
+    B = np.ascontiguousarray(g['B'])
+    basis = torch.tensor(B, dtype=torch.float32, device=cuda)
+    gen = torch.Generator(device=cuda).manual_seed(3)
+    theta = torch.randn(8, B.shape[1], device=cuda, generator=gen)
+    A, _, E = N.cell_tables([4, 4, 4], NSTEPS, theta, basis)
+    pts = torch.rand(8, 3, 20000, device=cuda, generator=gen)
+    cot = torch.randn(8, 3, 20000, device=cuda, generator=gen)
+    ws_glob = N.load().cpab_backward_workspace(3, N._ints([4, 4, 4]), NSTEPS, 20000, 8)
+    assert ws_glob > 8 * 320 * 12 * 4 * 4        # partials plus per-warp tables
+    ref_dth, ref_dp = N.backward([4, 4, 4], NSTEPS, mode, pts, A, E, basis, cot, want_dpoints=True)
+    rc, dth, dp = _noalloc(N, [4, 4, 4], mode, pts, A, E, basis, cot)
+    assert rc == 0, N.load().cpab_last_error()
+    assert torch.equal(dp, ref_dp)
+    assert _rel(dth, ref_dth) <= 1e-5
+    assert N.device_status() == 0
+
+
 def test_noalloc_rejects_oversized_problem(cuda):
     """n_theta * nC * ndim*(ndim+1) above the fixed scratch is refused with a
     clear error, before any work is enqueued."""
