@@ -172,6 +172,15 @@ def time_events(fn, steps, flush=None, stream=None):
     return times
 
 
+def workload_config(batch):
+    """The headline workload, shared by both arms' JSON lines."""
+    return {'workload': 'transform_data 2D tess [3,3] zero_boundary, 64 theta ~ N(0,0.25I), '
+                        'data [64,3,224,224] box-filtered U[0,1], MSE vs second warp, '
+                        'fwd + dtheta/d(data) bwd',
+            'tess_size': NC, 'batch': batch, 'outsize': [SIZE, SIZE], 'nstepsolver': NSTEPS,
+            'gradient': 'reference'}
+
+
 def run_gb300(args):
     from libcpab_gb300 import Cpab, _native as N
     from libcpab_gb300.functions import basis_on
@@ -332,11 +341,7 @@ def run_gb300(args):
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms_max,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
             'dtype': 'f32', 'data': 'synthetic',
-            'config': {'workload': 'transform_data 2D tess [3,3] zero_boundary, 64 theta ~ '
-                                   'N(0,0.25I), data [64,3,224,224] box-filtered U[0,1], '
-                                   'MSE vs second warp, fwd + dtheta/d(data) bwd',
-                       'tess_size': NC, 'batch': args.batch, 'outsize': [SIZE, SIZE],
-                       'nstepsolver': NSTEPS, 'gradient': params.gradient,
+            'config': {**workload_config(args.batch),
                        'l2': 'flushed before every timed iteration (%d MB write)'
                              % (2 * L2_BYTES // 2 ** 20),
                        'parallelism': 'dp%d' % world,
@@ -774,9 +779,10 @@ def main():
                 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
                 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
                 'dtype': 'f32', 'data': 'synthetic',
-                'config': {'workload': 'transform_data 2D tess [3,3], 224x224, MSE fwd + '
-                                       'reference analytic dtheta + d(data) backward',
-                           'parallelism': 'cpu'},
+                'config': {**workload_config(BATCH), 'parallelism': 'cpu',
+                           'step': "the reference's CPU implementation (its C++ op and "
+                                   "interpolation, restated in oracle/) on a sample of the "
+                                   "batch, see cpu_baseline.sample"},
                 'cpu_baseline': {'value': v, 'unit': 'points/s', 'cores': cores,
                                  'kind': 'port', 'sample': sample},
                 'e2e': {'value': v, 'unit': 'points/s', 'h2d_bytes_per_step': 0,
