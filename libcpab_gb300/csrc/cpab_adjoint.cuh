@@ -20,7 +20,10 @@ inline Steps make_steps(int nsteps) {
     return st;
 }
 
-// One forward step of the trajectory that the adjoint differentiates.
+// One forward step of the trajectory that the adjoint differentiates,
+// p += M [p; 1] with the cell's map from the table: E in mode 1 (the
+// compensated step of k_integrate), the midpoint-rule step map in mode 0
+// (build_dtab turns A into it).
 template <int N, int MODE>
 __device__ __forceinline__ void traj_step(const float *tab, int c, const Steps &st,
                                           float (&p)[N]) {
@@ -28,17 +31,8 @@ __device__ __forceinline__ void traj_step(const float *tab, int c, const Steps &
     float M[P], y[N];
     load_cell<N>(tab, c, M);
     affine_apply<N>(M, p, y);
-    if constexpr (MODE == 1) {
 #pragma unroll
-        for (int r = 0; r < N; ++r) p[r] += y[r];
-    } else {
-        float pm[N], vm[N];
-#pragma unroll
-        for (int r = 0; r < N; ++r) pm[r] = fmaf(st.hh, y[r], p[r]);
-        affine_apply<N>(M, pm, vm);
-#pragma unroll
-        for (int r = 0; r < N; ++r) p[r] = fmaf(st.h, vm[r], p[r]);
-    }
+    for (int r = 0; r < N; ++r) p[r] += y[r];
 }
 
 // Row stride of the per-cell adjoint propagator table (16-byte aligned rows
@@ -49,29 +43,43 @@ __host__ __device__ constexpr int dtab_stride() { return N == 1 ? 1 : (N == 2 ? 
 // Per-cell propagator of the adjoint, D with lambda_n = lambda_{n+1} + D^T lambda_{n+1}:
 //   mode 0: D = h A_lin + h^2/2 A_lin^2  (M - I of the midpoint sensitivity)
 //   mode 1: D = E_lin                     (the linear part of T - I)
-// stored row-major, D[r][k] at dtab[c * stride + r * N + k].  Cells are
-// split over the calling threads (first, first + stride, ...); the caller
+// stored row-major, D[r][k] at dtab[c * stride + r * N + k].
+// In mode 0 the cell table is then turned, in place, from A into the step
+// map of the midpoint rule, which for an affine field is itself affine:
+// p + h A~(p~ + h/2 A~ p~) = p + (h A~ + h^2/2 A~^2) p~ (A~ = [A; 0]), so
+// traj_step applies one map per step (its linear part is D).  Cells are split
+// over the calling threads (first, first + stride, ...); the caller
 // synchronises.
 template <int N, int MODE>
-__device__ __forceinline__ void build_dtab(const float *tab, float *dtab, int nC, const Steps &st,
+__device__ __forceinline__ void build_dtab(float *tab, float *dtab, int nC, const Steps &st,
                                            int first, int stride) {
     constexpr int P = N * (N + 1);
     for (int c = first; c < nC; c += stride) {
-        const float *a = tab + c * P;
+        float *a = tab + c * P;
         float *d = dtab + c * dtab_stride<N>();
+        if constexpr (MODE == 1) {
 #pragma unroll
-        for (int r = 0; r < N; ++r)
+            for (int r = 0; r < N; ++r)
 #pragma unroll
-            for (int k = 0; k < N; ++k) {
-                if constexpr (MODE == 1) {
-                    d[r * N + k] = a[r * (N + 1) + k];
-                } else {
+                for (int k = 0; k < N; ++k) d[r * N + k] = a[r * (N + 1) + k];
+        } else {
+            float m2[P];
+#pragma unroll
+            for (int r = 0; r < N; ++r)
+#pragma unroll
+                for (int k = 0; k <= N; ++k) {
                     float s = 0.f;
 #pragma unroll
                     for (int m = 0; m < N; ++m) s = fmaf(a[r * (N + 1) + m], a[m * (N + 1) + k], s);
-                    d[r * N + k] = fmaf(st.h, a[r * (N + 1) + k], st.hh2 * s);
+                    m2[r * (N + 1) + k] = fmaf(st.h, a[r * (N + 1) + k], st.hh2 * s);
                 }
-            }
+#pragma unroll
+            for (int r = 0; r < N; ++r)
+#pragma unroll
+                for (int k = 0; k < N; ++k) d[r * N + k] = m2[r * (N + 1) + k];
+#pragma unroll
+            for (int i = 0; i < P; ++i) a[i] = m2[i];
+        }
     }
 }
 
