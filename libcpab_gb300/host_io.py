@@ -2,11 +2,12 @@
 
 A caller whose inputs live in (pinned) host memory would otherwise copy a
 whole batch to the GPU before the first kernel starts.  HostUpload issues the
-copy on a side stream in batch chunks and records one event per chunk;
-transform_data_from_host (functions.py) starts the fused forward of chunk k
-as soon as chunk k has arrived, so the copy of the rest of the batch runs
-under the forward of the first chunks.  Everything stays stream-ordered (no
-host synchronisation), so it can also be captured in a CUDA graph.
+copy on a side stream (optionally in batch chunks, one event per chunk).
+transform_data_from_host (functions.py) queues the integration of the
+trajectories first (it needs no image), then the copy of the images, and
+samples once the copy has landed, so the copy runs under the integration.
+Everything stays stream-ordered (no host synchronisation), so it can also be
+captured in a CUDA graph.
 """
 from __future__ import annotations
 
