@@ -91,9 +91,9 @@ static bool plan_t(const Tess &t, int nsteps, long long nP, int n_theta, Adjoint
     int block = 0, per_sm = 0;
     bool global_gw = false;
     size_t smem = 0;
-    // global per-warp tables only in 3D, where the tables are large
+    // global per-warp tables in 2D and 3D, where the tables can be large
     decltype(&k_adjoint<N, MODE, CT, false>) kg = nullptr;
-    if constexpr (N == 3)
+    if constexpr (N >= 2)
         if (allow_global) kg = k_adjoint<N, MODE, CT, true>;
     if (!adjoint_shape<N, CT>(k_adjoint<N, MODE, CT, false>, kg, t.nC, nsteps, &block,
                               &global_gw, &smem, &per_sm))
@@ -144,7 +144,7 @@ static cudaError_t launch_adjoint_t(const Tess &t, int nsteps, const AdjointPlan
                                     float *dpoints, float *partials, unsigned long long *ties,
                                     unsigned *err, cudaStream_t s) {
     auto kern = k_adjoint<N, MODE, CT, false>;
-    if constexpr (N == 3)
+    if constexpr (N >= 2)
         if (plan.gw_floats) kern = k_adjoint<N, MODE, CT, true>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)plan.smem);

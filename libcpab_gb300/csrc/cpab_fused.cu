@@ -231,9 +231,9 @@ static bool plan_td_t(const Tess &t, int nsteps, long long nP, int nb, AdjointPl
     int block = 0, per_sm = 0;
     bool global_gw = false;
     size_t smem = 0;
-    // global per-warp tables only in 3D, where the tables are large
+    // global per-warp tables in 2D and 3D, where the tables can be large
     decltype(&k_transform_data_backward<N, MODE, CT, false>) kg = nullptr;
-    if constexpr (N == 3) kg = k_transform_data_backward<N, MODE, CT, true>;
+    if constexpr (N >= 2) kg = k_transform_data_backward<N, MODE, CT, true>;
     if (!adjoint_shape<N, CT>(k_transform_data_backward<N, MODE, CT, false>, kg, t.nC, nsteps,
                               &block, &global_gw, &smem, &per_sm))
         return false;
@@ -277,7 +277,7 @@ static cudaError_t launch_td_bwd_t(const Tess &t, int nsteps, const AdjointPlan 
                                    const float *gout, float *ddata, float *partials,
                                    unsigned long long *ties, unsigned *err, cudaStream_t s) {
     auto kern = k_transform_data_backward<N, MODE, CT, false>;
-    if constexpr (N == 3)
+    if constexpr (N >= 2)
         if (plan.gw_floats) kern = k_transform_data_backward<N, MODE, CT, true>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)plan.smem);
