@@ -111,9 +111,19 @@ def _check(rc: int):
         raise CpabError('libcpab_gb300 error %d: %s' % (rc, msg))
 
 
+_ints_cache = {}
+
+
 def _ints(v):
-    v = [int(x) for x in v]
-    return (ctypes.c_int * len(v))(*v)
+    # the C side only reads these arrays, so one per distinct tuple is reused
+    # (the per-call host overhead sits on the critical path of eager steps)
+    key = tuple(int(x) for x in v)
+    a = _ints_cache.get(key)
+    if a is None:
+        if len(_ints_cache) > 256:
+            _ints_cache.clear()
+        a = _ints_cache[key] = (ctypes.c_int * len(key))(*key)
+    return a
 
 
 def _ptr(t):
@@ -136,10 +146,17 @@ def _require(t, name, dtype=torch.float32):
 
 
 # ----------------------------------------------------------------------------- #
+_cells_cache = {}
+
+
 def num_cells(nc) -> int:
-    n = load().cpab_num_cells(len(nc), _ints(nc))
-    if n < 0:
-        _check(1)
+    key = tuple(int(x) for x in nc)
+    n = _cells_cache.get(key)
+    if n is None:
+        n = load().cpab_num_cells(len(key), _ints(key))
+        if n < 0:
+            _check(1)
+        _cells_cache[key] = n
     return n
 
 

@@ -113,8 +113,8 @@ static bool plan_t(const Tess &t, int nsteps, long long nP, int n_theta, Adjoint
     return true;
 }
 
-bool plan_adjoint_mode(const Tess &t, int nsteps, int mode, long long nP, int n_theta,
-                       AdjointPlan *plan, bool allow_global) {
+static bool plan_adjoint_mode_uncached(const Tess &t, int nsteps, int mode, long long nP,
+                                       int n_theta, AdjointPlan *plan, bool allow_global) {
     const bool small = t.nC <= 256;
 #define CPAB_PLAN(N)                                                                          \
     if (mode == 0)                                                                            \
@@ -128,6 +128,16 @@ bool plan_adjoint_mode(const Tess &t, int nsteps, int mode, long long nP, int n_
         default: { CPAB_PLAN(3) }
     }
 #undef CPAB_PLAN
+}
+
+bool plan_adjoint_mode(const Tess &t, int nsteps, int mode, long long nP, int n_theta,
+                       AdjointPlan *plan, bool allow_global) {
+    static PlanCache cache;
+    return cache.get(0, t, nsteps, mode, nP, n_theta, allow_global ? 1 : 0, plan,
+                     [&](AdjointPlan *p) {
+                         return plan_adjoint_mode_uncached(t, nsteps, mode, nP, n_theta, p,
+                                                           allow_global);
+                     });
 }
 
 bool plan_adjoint(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan,

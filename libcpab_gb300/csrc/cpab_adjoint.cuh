@@ -2,6 +2,10 @@
 // fused transform_data backward (cpab_fused.cu).  The scheme is described at
 // the top of cpab_adjoint.cu.
 #pragma once
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "cpab_launch.h"
 
 namespace cpab {
@@ -188,6 +192,36 @@ inline bool adjoint_shape(K kern_shared, K kern_global, int nC, int nsteps, int 
     }
     return best > 0;
 }
+
+// Host: launch plans are computed once per problem shape and device (the
+// occupancy queries behind a plan cost tens of microseconds, on the critical
+// path of an eager training step).
+struct PlanCache {
+    using Key = std::tuple<int, int, int, int, int, int, int, long long, int, int, int>;
+    std::mutex mu;
+    std::map<Key, AdjointPlan> plans;
+
+    template <typename F>
+    bool get(int kind, const Tess &t, int nsteps, int mode, long long nP, int n, int flag,
+             AdjointPlan *plan, F compute) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const Key key(dev, kind, t.ndim, t.nc[0], t.nc[1], t.nc[2], nsteps, nP, n, mode, flag);
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            auto it = plans.find(key);
+            if (it != plans.end()) {
+                *plan = it->second;
+                return true;
+            }
+        }
+        if (!compute(plan)) return false;
+        std::lock_guard<std::mutex> lock(mu);
+        if (plans.size() > 4096) plans.clear();
+        plans[key] = *plan;
+        return true;
+    }
+};
 
 template <int N, typename CT>
 struct AdjSmem {

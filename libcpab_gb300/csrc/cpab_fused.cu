@@ -252,8 +252,8 @@ static bool plan_td_t(const Tess &t, int nsteps, long long nP, int nb, AdjointPl
     return true;
 }
 
-bool plan_transform_data_backward(const Tess &t, int nsteps, int mode, long long nP, int nb,
-                                  AdjointPlan *plan) {
+static bool plan_td_uncached(const Tess &t, int nsteps, int mode, long long nP, int nb,
+                             AdjointPlan *plan) {
     const bool small = t.nC <= 256;
 #define CPAB_PLAN(N)                                                                          \
     if (mode == 0)                                                                            \
@@ -267,6 +267,14 @@ bool plan_transform_data_backward(const Tess &t, int nsteps, int mode, long long
         default: { CPAB_PLAN(3) }
     }
 #undef CPAB_PLAN
+}
+
+bool plan_transform_data_backward(const Tess &t, int nsteps, int mode, long long nP, int nb,
+                                  AdjointPlan *plan) {
+    static PlanCache cache;
+    return cache.get(1, t, nsteps, mode, nP, nb, 0, plan, [&](AdjointPlan *p) {
+        return plan_td_uncached(t, nsteps, mode, nP, nb, p);
+    });
 }
 
 template <int N, int MODE, typename CT>
