@@ -50,7 +50,7 @@ extern "C" {
 
 /* Bits reported by cpab_device_status. */
 #define CPAB_DEV_TMA_TIMEOUT 1u /* a bulk copy to shared memory did not complete */
-#define CPAB_DEV_BAD_CELL 2u    /* a cell index fell outside [0, nC)             */
+#define CPAB_DEV_BAD_CELL 2u    /* reserved (every lookup returns a valid cell)  */
 #define CPAB_DEV_BAD_OFFSETS 8u /* a ragged series had invalid offsets (skipped) */
 #define CPAB_DEV_ITER_LIMIT 16u /* an exact-flow trajectory hit its step limit     */
 

@@ -437,10 +437,6 @@ __device__ __forceinline__ void e_sweep(const float *tabE, const Tess &t, int ns
     constexpr int P = N * (N + 1);
     for (int s = 0; s < nsteps; ++s) {
         int c = find_cell<N>(p, t, ties);
-        if ((unsigned)c >= (unsigned)t.nC) {
-            raise_error(err, kErrBadCell);
-            c = 0;
-        }
         float M[P], y[N];
         load_cell<N>(tabE, c, M);
         affine_apply<N>(M, p, y);
@@ -462,10 +458,6 @@ __device__ __forceinline__ void logged_forward(const AdjSmem<N, CT> &sm, const T
         const int end = min(n0 + kSeg, nsteps);
         for (int n = n0; n < end; ++n) {
             int c = find_cell<N>(p, t, ties);
-            if ((unsigned)c >= (unsigned)t.nC) {
-                raise_error(err, kErrBadCell);
-                c = 0;
-            }
             sm.cl[n * B + tid] = (CT)c;
             traj_step<N, MODE>(sm.tab, c, st, p);
         }

@@ -38,7 +38,7 @@ constexpr int kMaxDim = 3;
 // Bits of the device error word (read back by cpab_device_status()).
 enum : unsigned {
     kErrTmaTimeout = 1u << 0,   // a bulk copy into shared memory did not complete
-    kErrBadCell = 1u << 1,      // a cell index fell outside [0, nC)
+    kErrBadCell = 1u << 1,      // reserved: every lookup returns a cell in [0, nC)
     kErrBadOffsets = 1u << 3,   // a ragged series had invalid offsets (skipped)
     kErrIterLimit = 1u << 4,    // an exact-flow trajectory hit its step limit
 };
@@ -542,6 +542,12 @@ __device__ __forceinline__ int cell_3d(float p0, float p1, float p2, const Tess 
     return cell_3d_exact(p0, p1, p2, t);
 }
 
+// The cell of p with the reference's rules.  Every path returns an index in
+// [0, nC) for every input, NaN and infinities included: the FP32 paths clamp
+// the square (or interval) indices to [0, nc-1] and add a sub-cell index in
+// [0, 4) or [0, 5); the FP64 replicas clamp like the reference (NaN and
+// negative coordinates to 0, large ones to nc-1).  The kernels therefore
+// index their shared-memory tables with it unchecked.
 template <int N>
 __device__ __forceinline__ int find_cell(const float (&p)[N], const Tess &t,
                                          unsigned long long *ties) {

@@ -129,11 +129,7 @@ __device__ void exact_flow_nd(float (&p)[N], const float *tab, const Tess &t,
     float tr = 1.f;
     int it = 0;
     for (; it < kExactMaxIter && tr > 0.f; ++it) {
-        int c = find_cell<N>(p, t, ties);
-        if ((unsigned)c >= (unsigned)t.nC) {
-            raise_error(err, kErrBadCell);
-            break;
-        }
+        const int c = find_cell<N>(p, t, ties);
         float M[P];
         load_cell<N>(tab, c, M);
         float v[N], speed2 = 0.f, anorm2 = 0.f;

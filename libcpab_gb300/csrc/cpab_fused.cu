@@ -69,10 +69,6 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
         for (int j = 0; j < PPT; ++j) {
             int c = find_cell<N>(p[j], t, ties);
-            if ((unsigned)c >= (unsigned)t.nC) {
-                raise_error(err, kErrBadCell);
-                c = 0;
-            }
             float M[P], y[N];
             load_cell<N>(tab, c, M);
             affine_apply<N>(M, p[j], y);

@@ -45,11 +45,7 @@ __global__ void __launch_bounds__(256)
     for (int s = 0; s < nsteps; ++s) {
 #pragma unroll
         for (int j = 0; j < PPT; ++j) {
-            int c = find_cell<N>(p[j], t, ties);
-            if ((unsigned)c >= (unsigned)t.nC) {   // cannot happen for finite input
-                raise_error(err, kErrBadCell);
-                c = 0;
-            }
+            const int c = find_cell<N>(p[j], t, ties);
             if (trace && idx[j] < nP) trace[((long long)th * nP + idx[j]) * nsteps + s] = c;
             float M[P], y[N];
             load_cell<N>(tab, c, M);
