@@ -39,9 +39,9 @@ L2_BYTES = 129 * 2 ** 20
 # adjoint 37 flop/step; interpolation 8*C bytes (forward), 12*C (backward)
 FLOP_FWD_STEP, FLOP_ADJ_STEP = 17, 37
 # DRAM bytes (read + write) of one k_transform_data_backward launch per image,
-# from an ncu capture of 16 images (36.12 MB); traffic grows with the images
+# from an ncu capture of 16 images (36.06 MB); traffic grows with the images
 # processed
-BWD_DRAM_BYTES_PER_IMAGE = 36.12e6 / 16
+BWD_DRAM_BYTES_PER_IMAGE = 36.06e6 / 16
 
 
 def parse():
