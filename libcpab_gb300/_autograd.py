@@ -145,29 +145,29 @@ class Interpolate(torch.autograd.Function):
 
 class TransformData(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, data, theta, params, outsize, upload=None):
-        # upload: a host_io.HostUpload whose tensor is `data`, still arriving:
-        # the trajectories are integrated first (they need no image), then the
-        # stream waits for the copy and samples (split forward, same bits)
+    def forward(ctx, data, theta, params, outsize, staged=None):
+        # staged (functions.transform_data_from_host): `data` is still being
+        # copied (staged['upload']); the tables and the trajectories
+        # (staged['A'], ['E'], ['lin'], ['grid']: integrated before the copy
+        # was queued, they need no image) are ready, so the stream waits for
+        # the copy and samples (split forward, same bits as the fused one)
         data_c = data.detach().to(torch.float32).contiguous()
-        theta_c = theta.detach().to(torch.float32).contiguous()
-        dev = data.device
-        from .functions import grid_axes
-        lin = grid_axes(params, outsize, dev)
-        basis = _basis(params, dev)
-        A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis)
         mode = _mode(params)
         needs_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
         save_grid = needs_grad and mode == N.GRAD_REFERENCE
-        if upload is None:
+        if staged is None:
+            theta_c = theta.detach().to(torch.float32).contiguous()
+            dev = data.device
+            from .functions import grid_axes
+            lin = grid_axes(params, outsize, dev)
+            A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, _basis(params, dev))
             out, grid = N.transform_data(params.nc, params.nstepsolver, lin, outsize, E, data_c,
                                          save_grid=save_grid, ties=_ties(params))
         else:
+            upload = staged['upload']
             if data_c.data_ptr() != upload.tensor.data_ptr():
                 raise ValueError('data must be the uploaded tensor')
-            grid = N.transform_grid_image(params.nc, params.nstepsolver, lin, outsize, E,
-                                          ties=_ties(params))
-            upload.start()   # the integration is already queued
+            A, E, lin, grid = staged['A'], staged['E'], staged['lin'], staged['grid']
             upload.wait()
             out = N.sample_grid(data_c, grid, outsize)
             if not save_grid:

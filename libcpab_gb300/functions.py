@@ -224,9 +224,21 @@ def transform_data_from_host(data, theta, params, outsize, requires_grad=False):
     if params.numeric_grad or getattr(params, 'integration', 'fixed_step') == 'exact':
         dev = HostUpload(data, theta.device).wait().requires_grad_(requires_grad)
         return transform_data(dev, theta, params, outsize), dev
-    up = HostUpload(data, theta.device, start=False)   # copied once the integration is queued
+    # queue the tables and the integration first (no image needed), then the
+    # copy of the images on the side stream, then the sampling (in the
+    # autograd Function, which also saves what the backward needs)
+    from ._autograd import _ties
+    device = theta.device
+    lin = grid_axes(params, outsize, device)
+    A, _, E = N.cell_tables(params.nc, params.nstepsolver,
+                            theta.detach().to(torch.float32).contiguous(),
+                            basis_on(params, device))
+    grid = N.transform_grid_image(params.nc, params.nstepsolver, lin, outsize, E,
+                                  ties=_ties(params))
+    up = HostUpload(data, device)
     dev = up.tensor.requires_grad_(requires_grad)
-    return TransformData.apply(dev, theta, params, outsize, up), dev
+    staged = {'upload': up, 'A': A, 'E': E, 'lin': lin, 'grid': grid}
+    return TransformData.apply(dev, theta, params, outsize, staged), dev
 
 
 def _check_ragged(values, offsets, theta, params):
