@@ -23,6 +23,8 @@
 //     sums S per cell and propagates lambda with the per-cell D = M - I;
 //     k_finalize applies G = h S (I + h/2 [A;0])^T + h^2/2 A_lin^T S once per
 //     cell.  The result is the reference's analytic gradient up to rounding.
+//     The trajectory is stepped with the equivalent single affine map
+//     p' = p + (h A~ + h^2/2 A~^2)[p;1] per cell (A~ = [A;0]; build_dtab).
 //   mode 1 ("exact"): exact discrete adjoint of the forward map
 //     p' = p + E_c [p;1]:  dL/dT_c += lambda_{n+1} [p_n;1]^T,
 //     lambda_n = lambda_{n+1} + E_lin^T lambda_{n+1}; dL/dA then follows from
@@ -41,7 +43,11 @@
 // step order.  At the end the warp copies are summed in warp order into one
 // partial per CTA, and k_finalize sums the partials in CTA order.  No
 // floating-point atomics are used, so the result is bit-reproducible for a
-// given GPU and input.
+// given GPU and input.  In 1D, where the lanes of a sorted grid sit in
+// non-decreasing cells, the lane groups are found without match.any
+// (warp_flush_1d).  For large tessellations the per-warp tables live in the
+// workspace instead of shared memory when that fits more warps per SM
+// (adjoint_shape, carve_adjoint).
 #include "cpab_adjoint.cuh"
 
 namespace cpab {
