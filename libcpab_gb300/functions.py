@@ -142,7 +142,8 @@ def grid_axes(params, outsize, device):
         return t
     t = torch.cat([torch.linspace(params.domain_min[i], params.domain_max[i], outsize[i],
                                   device=device) for i in range(params.ndim)]).contiguous()
-    if not torch.cuda.is_current_stream_capturing():
+    capturing = torch.device(device).type == 'cuda' and torch.cuda.is_current_stream_capturing()
+    if not capturing:
         if len(cache) >= 16:
             cache.clear()
         cache[key] = t

@@ -109,3 +109,19 @@ def test_ragged_points_argument_checks():
                      (meta(2, 20), meta(3, dtype=torch.int64), meta(3, 4))):
         with pytest.raises(ValueError):
             functions._check_ragged_points(p, o, th, T.params)
+
+
+def test_grid_axes_cached_and_equal_to_linspace():
+    from libcpab_gb300 import Cpab
+    from libcpab_gb300.functions import grid_axes
+    T = Cpab([3, 3], backend='pytorch', device='gpu')
+    a = grid_axes(T.params, (5, 7), 'cpu')
+    assert grid_axes(T.params, (5, 7), 'cpu') is a
+    assert torch.equal(a, torch.cat([torch.linspace(0, 1, 5), torch.linspace(0, 1, 7)]))
+    assert grid_axes(T.params, (7, 5), 'cpu') is not a
+
+
+def test_ints_and_cell_counts_are_reused():
+    from libcpab_gb300 import _native as N
+    assert N._ints([3, 3]) is N._ints((3, 3))
+    assert list(N._ints([4, 2, 8])) == [4, 2, 8]
