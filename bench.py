@@ -38,6 +38,10 @@ L2_BYTES = 129 * 2 ** 20
 # algorithmic work per point trajectory (2D, 50 steps): forward 17 flop/step,
 # adjoint 37 flop/step; interpolation 8*C bytes (forward), 12*C (backward)
 FLOP_FWD_STEP, FLOP_ADJ_STEP = 17, 37
+# thread instructions per point-step of the fused kernels (2D [3,3]), from the
+# ncu capture of 16 images summarised in profiles/ (smsp__inst_executed x
+# active threads per instruction / point-steps)
+INSTR_FWD_STEP, INSTR_BWD_STEP = 73, 159
 # DRAM bytes (read + write) of one k_transform_data_backward launch per image,
 # from an ncu capture of 16 images (36.06 MB); traffic grows with the images
 # processed
@@ -367,6 +371,21 @@ def run_gb300(args):
                          'traffic': BWD_DRAM_BYTES_PER_IMAGE * args.batch,
                          'traffic_unit': 'bytes per launch (ncu dram read+write, 16-image '
                                          'capture scaled by images)'},
+            'issue_roofline': {
+                'kernel': 'k_transform_data_backward (+finalize)',
+                'bound': 'instruction issue (the lookups and the adjoint are branchy scalar '
+                         'FP32/integer work, not FMA streams)',
+                'warp_instr_per_launch': pts * NSTEPS * INSTR_BWD_STEP / 32,
+                'achieved': pts * NSTEPS * INSTR_BWD_STEP / 32 / (bwd_ms / 1e3),
+                'peak': 152 * 4 * sm_mhz * 1e6,
+                'unit': 'warp instructions/s',
+                'frac': pts * NSTEPS * INSTR_BWD_STEP / 32 / (bwd_ms / 1e3)
+                        / (152 * 4 * sm_mhz * 1e6),
+                'forward_frac': pts * NSTEPS * INSTR_FWD_STEP / 32 / (fwd_ms / 1e3)
+                                / (152 * 4 * sm_mhz * 1e6),
+                'source': 'instructions per point-step from ncu (%d bwd, %d fwd); peak = '
+                          '152 SMs x 4 schedulers x 1 instruction/cycle at the sampled SM '
+                          'clock' % (INSTR_BWD_STEP, INSTR_FWD_STEP)},
             'forward_kernel': {'name': 'k_transform_data', 'ms_per_launch': fwd_ms,
                                'flop_per_launch': pts * NSTEPS * FLOP_FWD_STEP,
                                'tflops': pts * NSTEPS * FLOP_FWD_STEP / (fwd_ms / 1e3) / 1e12,
