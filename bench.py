@@ -60,7 +60,8 @@ def parse():
                          'are for profiling runs only)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--leg', default='all',
-                    choices=['all', 'ragged', 'volume', 'interp', 'aligner', 'exact', 'points'],
+                    choices=['all', 'ragged', 'volume', 'interp', 'aligner', 'exact', 'points',
+                             'mixed'],
                     help='run only one of the side workloads and print its result (for '
                          'profiling runs)')
     ap.add_argument('--no-tune', action='store_true',
@@ -323,6 +324,7 @@ def run_gb300(args):
     aligner = run_aligner(device) if extra else None
     exact = run_exact_flow(device, args.steps, flush) if extra else None
     points = run_ragged_points(device, args.steps, flush) if extra else None
+    mixed = run_mixed_images(device, args.steps, flush) if extra else None
     clk = clocks.stop() if clocks else None
     status = N.device_status()
 
@@ -402,6 +404,7 @@ def run_gb300(args):
             'aligner': aligner,
             'exact_flow': exact,
             'ragged_points_2d': points,
+            'mixed_size_images_2d': mixed,
             'clocks': clk, 'device_status': status,
         }
     if world > 1:
@@ -550,6 +553,56 @@ def run_ragged_points(device, steps, flush):
                        'tess [3,3] zero_boundary, theta ~ N(0,0.25I) per set; forward and '
                        'forward+dtheta (reference gradient), one persistent launch each'
                        % (POINTS_S, POINTS_LEN[0], POINTS_LEN[1], total))
+    return res
+
+
+MIXED_S, MIXED_SIDE = 64, (128, 320)
+
+
+def run_mixed_images(device, steps, flush):
+    """Images of mixed sizes: 64 images [3, W, H] with W, H ~ U{128..320}
+    (values U[0,1]), each warped to its own size by its own theta ~
+    N(0, 0.25 I), tess [3,3] zero_boundary.  One step = forward + backward
+    (reference gradient, dtheta and d(images)) of sum(out_s * w_s) through
+    Cpab.transform_data_mixed (one ragged integration launch, one ragged
+    sampling launch, and their adjoints); beside it the same step as a loop of
+    per-image transform_data calls (what the reference's API allows)."""
+    from libcpab_gb300 import Cpab
+    T = Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True)
+    T.set_solver_params(nstepsolver=NSTEPS)
+    g = torch.Generator().manual_seed(5)
+    sides = torch.randint(MIXED_SIDE[0], MIXED_SIDE[1] + 1, (MIXED_S, 2), generator=g).tolist()
+    ims = [torch.rand(CHANNELS, w, h, generator=g).to(device) for w, h in sides]
+    ws = [torch.randn(CHANNELS, w, h, generator=g).to(device) for w, h in sides]
+    theta = (THETA_STD * torch.randn(MIXED_S, T.get_theta_dim(), generator=g)).to(device)
+    total = sum(w * h for w, h in sides)
+
+    def step_mixed():
+        th = theta.detach().requires_grad_(True)
+        dd = [im.detach().requires_grad_(True) for im in ims]
+        torch.autograd.backward(T.transform_data_mixed(dd, th), ws)
+        return th.grad
+
+    def step_loop():
+        th = theta.detach().requires_grad_(True)
+        for s in range(MIXED_S):
+            d = ims[s][None].detach().requires_grad_(True)
+            torch.autograd.backward(T.transform_data(d, th[s:s + 1], sides[s]), ws[s][None])
+        return th.grad
+
+    res = {}
+    for tag, fn in (('mixed', step_mixed), ('per_image_loop', step_loop)):
+        for _ in range(3):
+            fn()
+        t = time_events(fn, steps, flush)
+        ms = sum(t) / len(t)
+        res[tag] = {'ms_per_step': ms, 'fwd_bwd_points_per_s': total / (ms / 1e3)}
+    a, b = step_mixed(), step_loop()
+    res['dtheta_rel_diff'] = float((a - b).abs().max() / b.abs().max())
+    res['workload'] = ('images of mixed sizes: %d images [%d, W, H], W, H ~ U{%d..%d} (total %d '
+                       'points), each warped to its size by its own theta ~ N(0,0.25I), tess '
+                       '[3,3] zero_boundary; forward + backward (dtheta, d(images)) of '
+                       'sum(out * w)' % (MIXED_S, CHANNELS, MIXED_SIDE[0], MIXED_SIDE[1], total))
     return res
 
 
@@ -818,7 +871,8 @@ def main():
               'interp': lambda: run_interp_sweep(device, args.steps, flush),
               'aligner': lambda: run_aligner(device),
               'exact': lambda: run_exact_flow(device, args.steps, flush),
-              'points': lambda: run_ragged_points(device, args.steps, flush)}[args.leg]
+              'points': lambda: run_ragged_points(device, args.steps, flush),
+              'mixed': lambda: run_mixed_images(device, args.steps, flush)}[args.leg]
         print(json.dumps({'leg': args.leg, 'result': fn()}))
         return
     res = run_gb300(args)

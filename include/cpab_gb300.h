@@ -399,6 +399,52 @@ CPAB_API int cpab_ragged_points_backward(int ndim, const int *nc, int nsteps, in
                                          unsigned long long *ties, void *stream);
 
 /*
+ * Ragged images: S images of mixed sizes (each with its own size and
+ * outsize, same C and ndim) sampled in one launch.  Replaces a loop of
+ * libcpab/pytorch/interpolation.py:12-172 calls (one data size and one
+ * outsize per call, :39-40), i.e. the sampling half of a loop of
+ * transform_data calls (libcpab/cpab.py:304-331) over images of different
+ * sizes; no counterpart in the reference.
+ *
+ * cpab_ragged_images_plan (host only, no CUDA call) fills plan, a HOST array
+ * of (S + 1) * CPAB_IMAGE_PLAN_FIELDS int64: row s = [data_off, pts_off,
+ * tile_off, size[3], outsize[3], 0] with the extents padded with 1, and row
+ * S = [data_points, total, tiles, 0, ...].  sizes and outsizes are host
+ * [S, ndim] (outsizes NULL: each image keeps its size).  totals[3] receives
+ * data_points (sum of prod(size)), total (sum of prod(outsize), below 2^31)
+ * and tiles.  The caller copies the plan to the device once and passes it
+ * with those totals to the calls below (the kernels check the rows they use
+ * and raise CPAB_DEV_BAD_OFFSETS on a row that does not fit them).
+ *
+ * Layout: data packs the [C, size_s] blocks (image s at C * data_off[s]);
+ * grid is [ndim, total] with image s in the columns pts_off[s] ..
+ * pts_off[s] + prod(outsize_s) in meshgrid order (x fastest), e.g. the
+ * output of cpab_ragged_points_forward with offsets = the plan's pts_off
+ * column; out packs the [C, outsize_s] blocks (image s at C * pts_off[s]).
+ * Each image's output is bit-identical to cpab_interpolate on that image.
+ */
+#define CPAB_IMAGE_PLAN_FIELDS 10
+CPAB_API int cpab_ragged_images_plan(int ndim, int S, const int *sizes, const int *outsizes,
+                                     long long *plan, long long *totals);
+
+CPAB_API int cpab_interpolate_ragged(int ndim, int S, int C, const long long *plan,
+                                     long long data_points, long long total, long long tiles,
+                                     const float *data, const float *grid, float *out,
+                                     void *stream);
+
+/*
+ * Backward of cpab_interpolate_ragged from grad_out (out's layout): ddata
+ * (overwritten, may be NULL; scatter-add with float atomics like
+ * cpab_interpolate_backward) and dgrid [ndim, total] (overwritten, may be
+ * NULL).
+ */
+CPAB_API int cpab_interpolate_ragged_backward(int ndim, int S, int C, const long long *plan,
+                                              long long data_points, long long total,
+                                              long long tiles, const float *data,
+                                              const float *grid, const float *grad_out,
+                                              float *ddata, float *dgrid, void *stream);
+
+/*
  * Synchronise the current device and report the device error word (the
  * CPAB_DEV_* bits raised by kernels since the last clear).  clear != 0 resets
  * it.  Returns CPAB_OK, or CPAB_ERR_CUDA if the device reported an error.

@@ -251,3 +251,31 @@ class TransformGridRagged(torch.autograd.Function):
             _basis(params, points.device), grad.to(torch.float32).contiguous(),
             want_dpoints=want_p, ties=_ties(params))
         return dpoints, (dtheta if want_t else None), None, None
+
+
+class InterpolateRagged(torch.autograd.Function):
+    """Packed images of mixed sizes sampled at a ragged grid (one launch each
+    way); `layout` is a functions.ImageLayout."""
+
+    @staticmethod
+    def forward(ctx, data, grid, layout, C):
+        data_c = data.detach().to(torch.float32).contiguous()
+        grid_c = grid.detach().to(torch.float32).contiguous()
+        out = N.interpolate_ragged(layout.ndim, layout.plan, layout.totals, data_c, grid_c, C)
+        ctx.save_for_backward(data_c, grid_c)
+        ctx.layout = layout
+        ctx.C = C
+        return out
+
+    @staticmethod
+    @once_differentiable
+    def backward(ctx, grad):
+        data, grid = ctx.saved_tensors
+        want_d, want_g = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        if not (want_d or want_g):
+            return None, None, None, None
+        lay = ctx.layout
+        ddata, dgrid = N.interpolate_ragged_backward(lay.ndim, lay.plan, lay.totals, data, grid,
+                                                     ctx.C, grad.to(torch.float32).contiguous(),
+                                                     want_ddata=want_d, want_dgrid=want_g)
+        return ddata, dgrid, None, None

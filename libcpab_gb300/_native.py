@@ -70,6 +70,10 @@ _SIGS = {
                                     _vp], _i),
     'cpab_ragged_points_backward': ([_i, _c_int_p, _i, _i, _vp, _vp, _i, _vp, _ll, _vp, _i, _vp,
                                      _vp, _vp, _vp, _vp, _sz, _vp, _vp], _i),
+    'cpab_ragged_images_plan': ([_i, _i, _c_int_p, _c_int_p, _vp, _vp], _i),
+    'cpab_interpolate_ragged': ([_i, _i, _i, _vp, _ll, _ll, _ll, _vp, _vp, _vp, _vp], _i),
+    'cpab_interpolate_ragged_backward': ([_i, _i, _i, _vp, _ll, _ll, _ll, _vp, _vp, _vp, _vp, _vp,
+                                          _vp], _i),
 }
 
 EXPORTED = tuple(_SIGS)
@@ -617,3 +621,64 @@ def ragged_points_backward(nc, nsteps, mode, A, E, offsets, points, basis, grad_
                                               _ptr(dpoints), _ptr(ws), ws.numel(), _ptr(ties),
                                               _stream(dev)))
     return dtheta, dpoints
+
+
+# ------------------------ ragged images (mixed sizes) ----------------------- #
+IMAGE_PLAN_FIELDS = 10
+
+
+def ragged_images_plan(ndim, sizes, outsizes=None):
+    """Host plan of S images of mixed sizes (no CUDA call): (plan int64
+    [S + 1, IMAGE_PLAN_FIELDS], (data_points, total, tiles))."""
+    import numpy as np
+    S = len(sizes)
+    flat = [int(x) for sz in sizes for x in sz]
+    if len(flat) != S * ndim or (outsizes is not None and len(outsizes) != S):
+        raise ValueError('sizes and outsizes must be S tuples of %d extents' % ndim)
+    oflat = None if outsizes is None else [int(x) for sz in outsizes for x in sz]
+    if oflat is not None and len(oflat) != S * ndim:
+        raise ValueError('outsizes must be S tuples of %d extents' % ndim)
+    plan = np.zeros((S + 1) * IMAGE_PLAN_FIELDS, dtype=np.int64)
+    totals = np.zeros(3, dtype=np.int64)
+    sz_c = (ctypes.c_int * max(len(flat), 1))(*flat)
+    osz_c = None if oflat is None else (ctypes.c_int * max(len(oflat), 1))(*oflat)
+    _check(load().cpab_ragged_images_plan(int(ndim), S, sz_c, osz_c,
+                                          ctypes.c_void_p(plan.ctypes.data),
+                                          ctypes.c_void_p(totals.ctypes.data)))
+    return plan.reshape(S + 1, IMAGE_PLAN_FIELDS), tuple(int(x) for x in totals)
+
+
+def interpolate_ragged(ndim, plan, totals, data, grid, C):
+    """Sample the packed images `data` at `grid` [ndim, total] with the
+    device plan [S + 1, IMAGE_PLAN_FIELDS]; returns the packed output
+    [C * total]."""
+    _require(plan, 'plan', torch.int64)
+    _require(data, 'data')
+    _require(grid, 'grid')
+    data_points, total, tiles = totals
+    if data.numel() != C * data_points or grid.shape != (ndim, total):
+        raise ValueError('data must hold C * %d values and grid be [%d, %d]'
+                         % (data_points, ndim, total))
+    out = torch.empty(C * total, device=data.device, dtype=torch.float32)
+    _check(load().cpab_interpolate_ragged(int(ndim), plan.shape[0] - 1, int(C), _ptr(plan),
+                                          data_points, total, tiles, _ptr(data), _ptr(grid),
+                                          _ptr(out), _stream(data.device)))
+    return out
+
+
+def interpolate_ragged_backward(ndim, plan, totals, data, grid, C, grad_out, want_ddata=True,
+                                want_dgrid=True):
+    """(ddata like data or None, dgrid [ndim, total] or None)."""
+    _require(plan, 'plan', torch.int64)
+    _require(data, 'data')
+    _require(grid, 'grid')
+    _require(grad_out, 'grad_out')
+    data_points, total, tiles = totals
+    if grad_out.numel() != C * total:
+        raise ValueError('grad_out must hold C * %d values' % total)
+    ddata = torch.empty_like(data) if want_ddata else None
+    dgrid = torch.empty_like(grid) if want_dgrid else None
+    _check(load().cpab_interpolate_ragged_backward(
+        int(ndim), plan.shape[0] - 1, int(C), _ptr(plan), data_points, total, tiles, _ptr(data),
+        _ptr(grid), _ptr(grad_out), _ptr(ddata), _ptr(dgrid), _stream(data.device)))
+    return ddata, dgrid

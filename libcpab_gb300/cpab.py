@@ -243,6 +243,17 @@ class Cpab(object):
         return self.backend.transform_grid_ragged(points, offsets, theta, self.params,
                                                   sort_by_cell=sort_by_cell)
 
+    def transform_data_mixed(self, data, theta, outsize=None):
+        """Images of mixed sizes (extension; no reference counterpart): a list
+        of S images [C, *size_s] with theta [S, d]; image s comes out as
+        transform_data(data[s][None], theta[s:s+1], outsize_s)[0] would, with
+        one integration launch and one sampling launch for all images.
+        outsize: None (keep each size), one size, or a list of S sizes."""
+        self._check_type(theta); self._check_device(theta)
+        for im in data:
+            self._check_type(im); self._check_device(im)
+        return self.backend.transform_data_mixed(data, theta, self.params, outsize)
+
     def ragged_mse(self, values, target, offsets, theta, **kwargs):
         """Fused forward + mean-squared-error loss + backward for ragged 1D
         series (extension).  Returns a dict with loss, sse, dtheta, dvalues."""

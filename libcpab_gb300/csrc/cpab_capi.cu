@@ -323,6 +323,107 @@ int cpab_sample_grid(int ndim, const float *data, int nb, int C, const int *size
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "sample_grid launch");
 }
 
+// ------------------------- ragged images (mixed sizes) -----------------------
+static_assert(CPAB_IMAGE_PLAN_FIELDS == kImagePlanFields, "plan row width");
+
+int cpab_ragged_images_plan(int ndim, int S, const int *sizes, const int *outsizes,
+                            long long *plan, long long *totals) {
+    g_err[0] = 0;
+    if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3");
+    if (S < 0) return fail(CPAB_ERR_ARGUMENT, "need S >= 0");
+    if (!plan || !totals || (S > 0 && !sizes))
+        return fail(CPAB_ERR_ARGUMENT, "sizes, plan or totals is NULL");
+    constexpr int F = kImagePlanFields;
+    long long data_points = 0, total = 0, tiles = 0;
+    for (int s = 0; s < S; ++s) {
+        const int *sz = sizes + (long long)s * ndim;
+        const int *osz = outsizes ? outsizes + (long long)s * ndim : sz;
+        int rc = check_geo(ndim, sz, osz, 1);
+        if (rc) {
+            char why[sizeof g_err];
+            snprintf(why, sizeof why, "%s", g_err);
+            return fail(rc, "image %d: %s", s, why);
+        }
+        long long *row = plan + (long long)s * F;
+        row[0] = data_points;
+        row[1] = total;
+        row[2] = tiles;
+        long long nD = 1, nP = 1;
+        for (int j = 0; j < 3; ++j) {
+            row[3 + j] = j < ndim ? sz[j] : 1;
+            row[6 + j] = j < ndim ? osz[j] : 1;
+            nD *= row[3 + j];
+            nP *= row[6 + j];
+        }
+        row[9] = 0;
+        data_points += nD;
+        total += nP;
+        tiles += image_tile_count(ndim, osz);
+        if (total >= (1ll << 31) || data_points >= (1ll << 40))
+            return fail(CPAB_ERR_UNSUPPORTED,
+                        "ragged images: at most 2^31 - 1 output points and 2^40 data points");
+    }
+    long long *last = plan + (long long)S * F;
+    for (int f = 0; f < F; ++f) last[f] = 0;
+    last[0] = data_points;
+    last[1] = total;
+    last[2] = tiles;
+    totals[0] = data_points;
+    totals[1] = total;
+    totals[2] = tiles;
+    return CPAB_OK;
+}
+
+static int check_ragged_images(int ndim, int S, int C, const long long *plan,
+                               long long data_points, long long total, long long tiles) {
+    if (ndim < 1 || ndim > 3) return fail(CPAB_ERR_ARGUMENT, "ndim must be 1, 2 or 3");
+    if (S < 0 || C < 1 || data_points < 0 || total < 0 || tiles < 0)
+        return fail(CPAB_ERR_ARGUMENT, "need S >= 0, C >= 1 and non-negative totals");
+    if (total >= (1ll << 31) || tiles > total)
+        return fail(CPAB_ERR_UNSUPPORTED, "ragged images: total below 2^31 and tiles <= total");
+    if (tiles > 0 && (S == 0 || !plan)) return fail(CPAB_ERR_ARGUMENT, "plan is NULL");
+    return CPAB_OK;
+}
+
+int cpab_interpolate_ragged(int ndim, int S, int C, const long long *plan,
+                            long long data_points, long long total, long long tiles,
+                            const float *data, const float *grid, float *out, void *stream) {
+    g_err[0] = 0;
+    int rc = check_ragged_images(ndim, S, C, plan, data_points, total, tiles);
+    if (rc) return rc;
+    if (tiles == 0) return CPAB_OK;
+    if (!data || !grid || !out) return fail(CPAB_ERR_ARGUMENT, "data, grid or out is NULL");
+    unsigned *err = device_error_word();
+    if (!err) return fail(CPAB_ERR_CUDA, "device error word unavailable");
+    cudaError_t e = launch_interpolate_ragged(ndim, S, plan, data_points, data, C, total, tiles,
+                                              grid, out, err, as_stream(stream));
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "ragged interpolate launch");
+}
+
+int cpab_interpolate_ragged_backward(int ndim, int S, int C, const long long *plan,
+                                     long long data_points, long long total, long long tiles,
+                                     const float *data, const float *grid,
+                                     const float *grad_out, float *ddata, float *dgrid,
+                                     void *stream) {
+    g_err[0] = 0;
+    int rc = check_ragged_images(ndim, S, C, plan, data_points, total, tiles);
+    if (rc) return rc;
+    cudaStream_t s = as_stream(stream);
+    if (ddata && data_points > 0) {
+        cudaError_t e = cudaMemsetAsync(ddata, 0, (size_t)data_points * C * sizeof(float), s);
+        if (e != cudaSuccess) return cuda_fail(e, "memset");
+    }
+    if (tiles == 0) return CPAB_OK;
+    if (!data || !grid || !grad_out)
+        return fail(CPAB_ERR_ARGUMENT, "data, grid or grad_out is NULL");
+    unsigned *err = device_error_word();
+    if (!err) return fail(CPAB_ERR_CUDA, "device error word unavailable");
+    cudaError_t e = launch_interpolate_ragged_backward(ndim, S, plan, data_points, data, C, total,
+                                                       tiles, grid, grad_out, ddata, dgrid, err,
+                                                       s);
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "ragged interpolate backward launch");
+}
+
 size_t cpab_transform_data_backward_workspace(int ndim, const int *nc, int nsteps, int mode,
                                               const int *outsize, int nb) {
     g_err[0] = 0;

@@ -181,6 +181,27 @@ cudaError_t launch_ragged_points_backward(const Tess &t, int nsteps, int mode, i
 cudaError_t launch_sample_grid(int ndim, const float *grid, int nb, const float *data, int C,
                                const int *size, const int *outsize, float *out, cudaStream_t s);
 
+// Ragged images of mixed sizes (cpab_interp_ragged.cu).  Plan row s (int64):
+// [data_off, pts_off, tile_off, size[3], outsize[3], 0] (extents padded with
+// 1); row S holds the three totals.  Tiles of 256 points (1D) or 8 x-rows x
+// 32 last-axis columns (2D, and 3D at one y).
+constexpr int kImagePlanFields = 10;
+__host__ __device__ inline long long image_tile_count(int ndim, const int *outsize) {
+    if (ndim == 1) return (outsize[0] + 255ll) / 256;
+    const long long ta = (outsize[0] + 7ll) / 8, tz = (outsize[ndim - 1] + 31ll) / 32;
+    return ndim == 2 ? ta * tz : ta * tz * outsize[1];
+}
+cudaError_t launch_interpolate_ragged(int ndim, int S, const long long *plan,
+                                      long long data_points, const float *data, int C,
+                                      long long total, long long tiles, const float *grid,
+                                      float *out, unsigned *err, cudaStream_t s);
+cudaError_t launch_interpolate_ragged_backward(int ndim, int S, const long long *plan,
+                                               long long data_points, const float *data, int C,
+                                               long long total, long long tiles,
+                                               const float *grid, const float *gout,
+                                               float *ddata, float *dgrid, unsigned *err,
+                                               cudaStream_t s);
+
 int num_sms();
 
 }  // namespace cpab

@@ -321,6 +321,96 @@ def transform_grid_ragged(points, offsets, theta, params, sort_by_cell=False):
     return out[:, inv]
 
 
+class ImageLayout:
+    """Where S images of mixed sizes sit in the packed buffers of
+    transform_data_mixed: the device plan of cpab_ragged_images_plan, the
+    point-set offsets (its pts_off column) and the concatenated meshgrids
+    [ndim, total] of the outsizes."""
+
+    def __init__(self, params, sizes, outsizes, device):
+        self.ndim = params.ndim
+        self.sizes = [tuple(s) for s in sizes]
+        self.outsizes = [tuple(o) for o in outsizes]
+        plan, self.totals = N.ragged_images_plan(self.ndim, self.sizes, self.outsizes)
+        self.plan = torch.from_numpy(plan).to(device)
+        self.offsets = self.plan[:, 1].contiguous()
+        self.npoints = [int(plan[s + 1, 1] - plan[s, 1]) for s in range(len(self.sizes))]
+        grids = {}
+        for o in set(self.outsizes):
+            grids[o] = uniform_meshgrid(self.ndim, params.domain_min, params.domain_max, list(o),
+                                        device)
+        if self.outsizes:
+            self.points = torch.cat([grids[o] for o in self.outsizes], dim=1).contiguous()
+        else:
+            self.points = torch.empty((self.ndim, 0), device=device)
+
+
+def image_layout(params, sizes, outsizes, device):
+    """ImageLayout for these sizes, cached per (device, sizes, outsizes,
+    domain) outside CUDA-graph capture (like grid_axes)."""
+    key = (str(device), tuple(sizes), tuple(outsizes), tuple(params.domain_min[:params.ndim]),
+           tuple(params.domain_max[:params.ndim]))
+    cache = params.__dict__.setdefault('_layout_cache', {})
+    lay = cache.get(key)
+    if lay is not None:
+        return lay
+    lay = ImageLayout(params, sizes, outsizes, device)
+    capturing = torch.device(device).type == 'cuda' and torch.cuda.is_current_stream_capturing()
+    if not capturing:
+        if len(cache) >= 16:
+            cache.clear()
+        cache[key] = lay
+    return lay
+
+
+def _mixed_outsizes(ndim, sizes, outsize):
+    if outsize is None:
+        return list(sizes)
+    outsize = list(outsize)
+    if len(outsize) == ndim and all(not isinstance(o, (list, tuple)) for o in outsize):
+        return [tuple(int(o) for o in outsize)] * len(sizes)
+    if len(outsize) != len(sizes):
+        raise ValueError('outsize must be None, one size of %d extents, or one per image' % ndim)
+    res = [tuple(int(x) for x in o) for o in outsize]
+    if any(len(o) != ndim for o in res):
+        raise ValueError('every outsize must have %d extents' % ndim)
+    return res
+
+
+def transform_data_mixed(data, theta, params, outsize=None):
+    """Images of mixed sizes, each warped by its own theta, in one
+    integration launch and one sampling launch: image s ([C, *size_s], all
+    with the same C) comes out exactly as transform_data(data[s][None],
+    theta[s:s+1], params, outsize_s)[0] would (libcpab/cpab.py:304-331).
+    outsize: None (each image keeps its size), one size for all images, or a
+    list of S sizes.  Returns the list of S outputs [C, *outsize_s];
+    gradients reach theta and the images."""
+    if params.numeric_grad or getattr(params, 'integration', 'fixed_step') == 'exact':
+        raise ValueError('transform_data_mixed runs the fixed-step scheme with the analytic '
+                         'gradient (numeric_grad=False, integration="fixed_step")')
+    data = list(data)
+    S = len(data)
+    if theta.dim() != 2 or theta.shape[0] != S:
+        raise ValueError('theta must be [n_images=%d, d]' % S)
+    if S == 0:
+        return []
+    _require_cuda(theta, *data)
+    ndim = params.ndim
+    C = data[0].shape[0] if data[0].dim() == ndim + 1 else -1
+    for im in data:
+        if im.dim() != ndim + 1 or im.shape[0] != C:
+            raise ValueError('every image must be [C, *%dD size] with the same C' % ndim)
+    sizes = [tuple(int(x) for x in im.shape[1:]) for im in data]
+    outsizes = _mixed_outsizes(ndim, sizes, outsize)
+    lay = image_layout(params, sizes, outsizes, theta.device)
+    from ._autograd import InterpolateRagged, TransformGridRagged
+    packed = torch.cat([im.reshape(-1).to(torch.float32) for im in data])
+    grid = TransformGridRagged.apply(lay.points, theta, lay.offsets, params)
+    out = InterpolateRagged.apply(packed, grid, lay, C)
+    return [o.view(C, *osz) for o, osz in zip(out.split([C * n for n in lay.npoints]),
+                                              lay.outsizes)]
+
+
 def findcellidx(ndim, p, nc):
     """Cell index of each column of p [ndim, nP] (int64), with the reference's
     C++/CUDA lookup rules (libcpab/core/cpab_ops.cpp:26-190)."""
