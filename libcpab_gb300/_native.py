@@ -625,6 +625,7 @@ def ragged_points_backward(nc, nsteps, mode, A, E, offsets, points, basis, grad_
 
 # ------------------------ ragged images (mixed sizes) ----------------------- #
 IMAGE_PLAN_FIELDS = 10
+RAGGED_MAX_LEN = 1 << 22   # points per set of the ragged point-set kernels
 
 
 def ragged_images_plan(ndim, sizes, outsizes=None):

@@ -9,6 +9,7 @@ module by name).
 """
 from __future__ import annotations
 
+import numpy as np
 import torch
 
 from . import _native as N
@@ -394,7 +395,6 @@ def transform_data_mixed(data, theta, params, outsize=None):
         raise ValueError('theta must be [n_images=%d, d]' % S)
     if S == 0:
         return []
-    _require_cuda(theta, *data)
     ndim = params.ndim
     C = data[0].shape[0] if data[0].dim() == ndim + 1 else -1
     for im in data:
@@ -402,6 +402,10 @@ def transform_data_mixed(data, theta, params, outsize=None):
             raise ValueError('every image must be [C, *%dD size] with the same C' % ndim)
     sizes = [tuple(int(x) for x in im.shape[1:]) for im in data]
     outsizes = _mixed_outsizes(ndim, sizes, outsize)
+    if any(int(np.prod(o)) >= N.RAGGED_MAX_LEN for o in outsizes):
+        raise ValueError('transform_data_mixed: every output must have fewer than %d points '
+                         '(the ragged integrator\'s per-set limit)' % N.RAGGED_MAX_LEN)
+    _require_cuda(theta, *data)
     lay = image_layout(params, sizes, outsizes, theta.device)
     from ._autograd import InterpolateRagged, TransformGridRagged
     packed = torch.cat([im.reshape(-1).to(torch.float32) for im in data])

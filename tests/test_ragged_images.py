@@ -202,6 +202,10 @@ def test_mixed_argument_checks():
     assert F.transform_data_mixed([], torch.zeros(0, T.get_theta_dim()), T.params) == []
     with pytest.raises(ValueError, match='CUDA'):
         F.transform_data_mixed([torch.zeros(1, 4, 4)] * 2, theta, T.params)
+    with pytest.raises(ValueError, match='same C'):
+        F.transform_data_mixed([torch.zeros(1, 4, 4), torch.zeros(2, 4, 4)], theta, T.params)
+    with pytest.raises(ValueError, match='fewer than'):
+        F.transform_data_mixed([torch.zeros(1, 4, 4)] * 2, theta, T.params, (2048, 2048))
     T.params.integration = 'exact'
     with pytest.raises(ValueError, match='fixed-step'):
         F.transform_data_mixed([torch.zeros(1, 4, 4)] * 2, theta, T.params)
