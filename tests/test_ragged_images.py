@@ -42,7 +42,7 @@ def _images(cuda, C, sizes, seed=1):
     return [torch.rand(C, *s, generator=gen).to(cuda) for s in sizes]
 
 
-def _check_mixed(T, cuda, C, sizes, outsize, scale=0.5, seed=0):
+def _check_mixed(T, cuda, C, sizes, outsize, scale=0.5, seed=0, ddata_tol=1e-5):
     gen = torch.Generator().manual_seed(seed)
     S = len(sizes)
     theta = (torch.randn(S, T.get_theta_dim(), generator=gen) * scale).to(cuda)
@@ -63,7 +63,7 @@ def _check_mixed(T, cuda, C, sizes, outsize, scale=0.5, seed=0):
         assert torch.equal(outs[s], ref[0]), 'image %d' % s
         (ref[0] * ws[s]).sum().backward()
         assert _rel(t1.grad[s], t2.grad[0]) <= 1e-4, 'dtheta of image %d' % s
-        assert _rel(d1[s].grad, d2.grad[0]) <= 1e-5, 'd(image) of image %d' % s
+        assert _rel(d1[s].grad, d2.grad[0]) <= ddata_tol, 'd(image) of image %d' % s
 
 
 # ------------------------------------------------------------------- GPU ---
@@ -93,11 +93,19 @@ def test_mixed_3d_matches_per_image(C, cuda):
 
 
 @pytest.mark.gpu
-def test_mixed_1d_matches_per_image(cuda):
+@pytest.mark.parametrize('zb,ddata_tol', [(True, 1e-5), (False, 1e-3)])
+def test_mixed_1d_matches_per_image(zb, ddata_tol, cuda):
+    """Without the zero boundary and with theta ~ N(0, I), most points of the
+    257-point series leave the domain and clamp to the edge pixel, where the
+    reference's weights (1 - xd, xd) reach about -164 and 165 (xd is taken
+    after the clamp) and cancel: ~400 float atomics of such terms into one
+    pixel differ with their order by ~1e-4 of the largest gradient, so d(image)
+    gets 1e-3 there (forward and dtheta keep their gates)."""
     from libcpab_gb300 import _native as N
-    T = _cpab([10], zb=False)
+    T = _cpab([10], zb=zb)
     N.device_status()
-    _check_mixed(T, cuda, 2, [(50,), (300,), (1,), (257,)], None, scale=1.0)
+    _check_mixed(T, cuda, 2, [(50,), (300,), (1,), (257,)], None, scale=1.0,
+                 ddata_tol=ddata_tol)
     assert N.device_status() == 0
 
 
