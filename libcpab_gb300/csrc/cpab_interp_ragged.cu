@@ -53,9 +53,9 @@ __device__ __forceinline__ bool image_tile(const long long *__restrict__ plan, i
     const long long *last = plan + (long long)S * F;
     if (t == 0 && threadIdx.x == 0 &&
         (plan[0] != 0 || plan[1] != 0 || last[1] != total || last[2] != (long long)gridDim.x))
-        atomicOr(err, kErrBadOffsets);   // the launch would not cover every point
+        raise_error(err, kErrBadOffsets);   // the launch would not cover every point
     if (!(plan[2] <= t && t < last[2])) {
-        atomicOr(err, kErrBadOffsets);
+        raise_error(err, kErrBadOffsets);
         return false;
     }
     int lo = 0, hi = S;   // plan[lo].tile <= t < plan[hi].tile
@@ -83,7 +83,7 @@ __device__ __forceinline__ bool image_tile(const long long *__restrict__ plan, i
          r1[2] - r0[2] == image_tile_count(N, outsize) && r1[0] <= data_points &&
          r1[1] <= total;
     if (!ok) {
-        atomicOr(err, kErrBadOffsets);
+        raise_error(err, kErrBadOffsets);
         return false;
     }
 #pragma unroll

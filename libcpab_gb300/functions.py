@@ -9,7 +9,6 @@ module by name).
 """
 from __future__ import annotations
 
-import numpy as np
 import torch
 
 from . import _native as N
@@ -364,6 +363,13 @@ def image_layout(params, sizes, outsizes, device):
     return lay
 
 
+def _count(extents):
+    n = 1
+    for e in extents:
+        n *= e
+    return n
+
+
 def _mixed_outsizes(ndim, sizes, outsize):
     if outsize is None:
         return list(sizes)
@@ -402,7 +408,7 @@ def transform_data_mixed(data, theta, params, outsize=None):
             raise ValueError('every image must be [C, *%dD size] with the same C' % ndim)
     sizes = [tuple(int(x) for x in im.shape[1:]) for im in data]
     outsizes = _mixed_outsizes(ndim, sizes, outsize)
-    if any(int(np.prod(o)) >= N.RAGGED_MAX_LEN for o in outsizes):
+    if any(_count(o) >= N.RAGGED_MAX_LEN for o in outsizes):
         raise ValueError('transform_data_mixed: every output must have fewer than %d points '
                          '(the ragged integrator\'s per-set limit)' % N.RAGGED_MAX_LEN)
     _require_cuda(theta, *data)
