@@ -566,7 +566,8 @@ def run_mixed_images(device, steps, flush):
     (reference gradient, dtheta and d(images)) of sum(out_s * w_s) through
     Cpab.transform_data_mixed (one ragged integration launch, one ragged
     sampling launch, and their adjoints); beside it the same step as a loop of
-    per-image transform_data calls (what the reference's API allows)."""
+    per-image transform_data calls (what the reference's API allows), and the
+    mixed step captured in a CUDA graph and replayed."""
     from libcpab_gb300 import Cpab
     T = Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True)
     T.set_solver_params(nstepsolver=NSTEPS)
@@ -599,6 +600,23 @@ def run_mixed_images(device, steps, flush):
         res[tag] = {'ms_per_step': ms, 'fwd_bwd_points_per_s': total / (ms / 1e3)}
     a, b = step_mixed(), step_loop()
     res['dtheta_rel_diff'] = float((a - b).abs().max() / b.abs().max())
+    # the mixed step captured once in a CUDA graph and replayed (the layout
+    # is cached by the eager calls above, so the capture only records kernels)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            step_mixed()
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        g_dth = step_mixed()
+    for _ in range(3):
+        graph.replay()
+    t = time_events(graph.replay, steps, flush)
+    ms = sum(t) / len(t)
+    res['mixed_graph'] = {'ms_per_step': ms, 'fwd_bwd_points_per_s': total / (ms / 1e3),
+                          'dtheta_equals_eager': bool(torch.equal(g_dth, a))}
     res['workload'] = ('images of mixed sizes: %d images [%d, W, H], W, H ~ U{%d..%d} (total %d '
                        'points), each warped to its size by its own theta ~ N(0,0.25I), tess '
                        '[3,3] zero_boundary; forward + backward (dtheta, d(images)) of '

@@ -127,6 +127,46 @@ def test_mixed_layout_is_cached_and_theta_only(cuda):
 
 
 @pytest.mark.gpu
+def test_mixed_cuda_graph_replay(cuda):
+    """Forward + backward of transform_data_mixed captured in a CUDA graph
+    (after an eager call has cached the layout): the replay reproduces the
+    eager outputs and dtheta bit for bit, and d(images) to float-atomic order."""
+    from libcpab_gb300 import _native as N
+    T = _cpab([3, 3])
+    sizes = [(17, 23), (32, 32), (40, 9)]
+    ims = _images(cuda, 2, sizes)
+    gen = torch.Generator().manual_seed(4)
+    theta = (torch.randn(3, T.get_theta_dim(), generator=gen) * 0.5).to(cuda)
+    ws = [torch.randn(2, *sz, generator=gen).to(cuda) for sz in sizes]
+
+    def step():
+        th = theta.detach().requires_grad_(True)
+        dd = [im.detach().requires_grad_(True) for im in ims]
+        outs = T.transform_data_mixed(dd, th)
+        torch.autograd.backward(outs, ws)
+        return [o.detach() for o in outs], th.grad, [d.grad for d in dd]
+
+    e_out, e_dth, e_dd = step()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        step()
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        g_out, g_dth, g_dd = step()
+    for _ in range(2):
+        g.replay()
+    torch.cuda.synchronize()
+    for x, y in zip(g_out, e_out):
+        assert torch.equal(x, y)
+    assert torch.equal(g_dth, e_dth)
+    for x, y in zip(g_dd, e_dd):
+        assert _rel(x, y) <= 1e-5
+    assert N.device_status() == 0
+
+
+@pytest.mark.gpu
 def test_bad_plan_rows_are_flagged_not_read(cuda):
     from libcpab_gb300 import _native as N
     plan, totals = N.ragged_images_plan(2, [(4, 4), (4, 4)])
