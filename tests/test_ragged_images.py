@@ -110,6 +110,33 @@ def test_mixed_1d_matches_per_image(zb, ddata_tol, cuda):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize('nc,sizes,outsizes', [
+    ([3, 3], [(17, 23), (64, 48), (1, 5)], [(9, 40), (64, 48), (3, 3)]),
+    ([2, 2, 2], [(9, 10, 11), (16, 8, 12)], [(9, 10, 11), (12, 9, 40)]),
+])
+def test_mixed_sampling_matches_c_oracle(nc, sizes, outsizes, cuda, oracle):
+    """Each image's output is the C oracle's interpolation (the reference's
+    fp32 formula, libcpab/pytorch/interpolation.py:18-172) of that image at
+    its warped grid, bit for bit."""
+    from libcpab_gb300 import _native as N
+    from libcpab_gb300.functions import basis_on, image_layout
+    T = _cpab(nc)
+    gen = torch.Generator().manual_seed(6)
+    theta = (torch.randn(len(sizes), T.get_theta_dim(), generator=gen) * 0.5).to(cuda)
+    ims = _images(cuda, 2, sizes, 7)
+    outs = T.transform_data_mixed(ims, theta, outsizes)
+    lay = image_layout(T.params, sizes, outsizes, cuda)
+    _, _, E = N.cell_tables(nc, NSTEPS, theta, basis_on(T.params, cuda))
+    grid = N.ragged_points_forward(nc, NSTEPS, E, lay.offsets, lay.points).cpu().numpy()
+    off = lay.offsets.cpu().numpy()
+    for s, (im, osz) in enumerate(zip(ims, outsizes)):
+        g = grid[:, off[s]:off[s + 1]][None]
+        ref = oracle.interpolate(im[None].cpu().numpy(), g, list(osz))
+        assert np.array_equal(outs[s].cpu().numpy(), ref[0]), 'image %d' % s
+    assert N.device_status() == 0
+
+
+@pytest.mark.gpu
 def test_mixed_layout_is_cached_and_theta_only(cuda):
     """Repeated calls with the same sizes reuse the device plan; theta without
     grad and images without grad run forward only."""
