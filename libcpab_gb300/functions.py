@@ -412,6 +412,8 @@ def transform_data_mixed(data, theta, params, outsize=None):
         raise ValueError('transform_data_mixed: every output must have fewer than %d points '
                          '(the ragged integrator\'s per-set limit)' % N.RAGGED_MAX_LEN)
     _require_cuda(theta, *data)
+    if any(im.device != theta.device for im in data):
+        raise ValueError('the images and theta must be on the same device (%s)' % theta.device)
     lay = image_layout(params, sizes, outsizes, theta.device)
     from ._autograd import InterpolateRagged, TransformGridRagged
     packed = torch.cat([im.reshape(-1).to(torch.float32) for im in data])
