@@ -381,6 +381,8 @@ static int check_ragged_images(int ndim, int S, int C, const long long *plan,
         return fail(CPAB_ERR_ARGUMENT, "need S >= 0, C >= 1 and non-negative totals");
     if (total >= (1ll << 31) || tiles > total)
         return fail(CPAB_ERR_UNSUPPORTED, "ragged images: total below 2^31 and tiles <= total");
+    if ((double)data_points * C >= 0x1p60 || (double)total * C >= 0x1p60)
+        return fail(CPAB_ERR_UNSUPPORTED, "ragged images: C * points must stay below 2^60");
     if (tiles > 0 && (S == 0 || !plan)) return fail(CPAB_ERR_ARGUMENT, "plan is NULL");
     return CPAB_OK;
 }
