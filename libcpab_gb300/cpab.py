@@ -254,6 +254,14 @@ class Cpab(object):
             self._check_type(im); self._check_device(im)
         return self.backend.transform_data_mixed(data, theta, self.params, outsize)
 
+    def transform_data_packed(self, data, sizes, theta, outsize=None):
+        """transform_data_mixed on images packed in one 1D buffer (their
+        [C, *size_s] blocks back to back, sizes: the S sizes); returns the
+        outputs' [C, *outsize_s] blocks back to back (extension)."""
+        self._check_type(data); self._check_device(data)
+        self._check_type(theta); self._check_device(theta)
+        return self.backend.transform_data_packed(data, sizes, theta, self.params, outsize)
+
     def ragged_mse(self, values, target, offsets, theta, **kwargs):
         """Fused forward + mean-squared-error loss + backward for ragged 1D
         series (extension).  Returns a dict with loss, sse, dtheta, dvalues."""

@@ -384,6 +384,29 @@ def _mixed_outsizes(ndim, sizes, outsize):
     return res
 
 
+def _check_mixed_mode(params):
+    if params.numeric_grad or getattr(params, 'integration', 'fixed_step') == 'exact':
+        raise ValueError('transform_data_mixed runs the fixed-step scheme with the analytic '
+                         'gradient (numeric_grad=False, integration="fixed_step")')
+
+
+def _mixed_layout(params, sizes, outsize, theta, tensors):
+    outsizes = _mixed_outsizes(params.ndim, sizes, outsize)
+    if any(_count(o) >= N.RAGGED_MAX_LEN for o in outsizes):
+        raise ValueError('transform_data_mixed: every output must have fewer than %d points '
+                         '(the ragged integrator\'s per-set limit)' % N.RAGGED_MAX_LEN)
+    _require_cuda(theta, *tensors)
+    if any(t.device != theta.device for t in tensors):
+        raise ValueError('the images and theta must be on the same device (%s)' % theta.device)
+    return image_layout(params, sizes, outsizes, theta.device)
+
+
+def _mixed_apply(packed, theta, params, lay, C):
+    from ._autograd import InterpolateRagged, TransformGridRagged
+    grid = TransformGridRagged.apply(lay.points, theta, lay.offsets, params)
+    return InterpolateRagged.apply(packed, grid, lay, C)
+
+
 def transform_data_mixed(data, theta, params, outsize=None):
     """Images of mixed sizes, each warped by its own theta, in one
     integration launch and one sampling launch: image s ([C, *size_s], all
@@ -392,9 +415,7 @@ def transform_data_mixed(data, theta, params, outsize=None):
     outsize: None (each image keeps its size), one size for all images, or a
     list of S sizes.  Returns the list of S outputs [C, *outsize_s];
     gradients reach theta and the images."""
-    if params.numeric_grad or getattr(params, 'integration', 'fixed_step') == 'exact':
-        raise ValueError('transform_data_mixed runs the fixed-step scheme with the analytic '
-                         'gradient (numeric_grad=False, integration="fixed_step")')
+    _check_mixed_mode(params)
     data = list(data)
     S = len(data)
     if theta.dim() != 2 or theta.shape[0] != S:
@@ -407,20 +428,36 @@ def transform_data_mixed(data, theta, params, outsize=None):
         if im.dim() != ndim + 1 or im.shape[0] != C:
             raise ValueError('every image must be [C, *%dD size] with the same C' % ndim)
     sizes = [tuple(int(x) for x in im.shape[1:]) for im in data]
-    outsizes = _mixed_outsizes(ndim, sizes, outsize)
-    if any(_count(o) >= N.RAGGED_MAX_LEN for o in outsizes):
-        raise ValueError('transform_data_mixed: every output must have fewer than %d points '
-                         '(the ragged integrator\'s per-set limit)' % N.RAGGED_MAX_LEN)
-    _require_cuda(theta, *data)
-    if any(im.device != theta.device for im in data):
-        raise ValueError('the images and theta must be on the same device (%s)' % theta.device)
-    lay = image_layout(params, sizes, outsizes, theta.device)
-    from ._autograd import InterpolateRagged, TransformGridRagged
+    lay = _mixed_layout(params, sizes, outsize, theta, data)
     packed = torch.cat([im.reshape(-1).to(torch.float32) for im in data])
-    grid = TransformGridRagged.apply(lay.points, theta, lay.offsets, params)
-    out = InterpolateRagged.apply(packed, grid, lay, C)
+    out = _mixed_apply(packed, theta, params, lay, C)
     return [o.view(C, *osz) for o, osz in zip(out.split([C * n for n in lay.npoints]),
                                               lay.outsizes)]
+
+
+def transform_data_packed(data, sizes, theta, params, outsize=None):
+    """transform_data_mixed on images already packed in one buffer: data is
+    1D, the [C, *size_s] blocks of the S images back to back; returns the
+    [C, *outsize_s] blocks of the outputs back to back (1D), and
+    back-propagates to data and theta.  Same values as transform_data_mixed,
+    without its per-image views (less host work per call)."""
+    _check_mixed_mode(params)
+    sizes = [tuple(int(x) for x in sz) for sz in sizes]
+    S = len(sizes)
+    if theta.dim() != 2 or theta.shape[0] != S:
+        raise ValueError('theta must be [n_images=%d, d]' % S)
+    if any(len(sz) != params.ndim for sz in sizes):
+        raise ValueError('every size must have %d extents' % params.ndim)
+    if data.dim() != 1:
+        raise ValueError('data must be 1D: the images\' [C, *size] blocks back to back')
+    if S == 0:
+        return data.new_zeros(0, dtype=torch.float32)
+    pix = sum(_count(sz) for sz in sizes)
+    if pix == 0 or data.numel() % pix:
+        raise ValueError('data holds %d values, not C x %d pixels' % (data.numel(), pix))
+    lay = _mixed_layout(params, sizes, outsize, theta, [data])
+    return _mixed_apply(data.to(torch.float32).contiguous(), theta, params, lay,
+                        data.numel() // pix)
 
 
 def findcellidx(ndim, p, nc):

@@ -137,6 +137,31 @@ def test_mixed_sampling_matches_c_oracle(nc, sizes, outsizes, cuda, oracle):
 
 
 @pytest.mark.gpu
+def test_packed_matches_mixed(cuda):
+    """transform_data_packed on the concatenated images gives the
+    concatenated outputs of transform_data_mixed, and the same gradients."""
+    T = _cpab([3, 3])
+    sizes = [(17, 23), (32, 32), (1, 5)]
+    outsizes = [(9, 40), (32, 32), (3, 3)]
+    ims = _images(cuda, 3, sizes, 9)
+    gen = torch.Generator().manual_seed(10)
+    theta = (torch.randn(3, T.get_theta_dim(), generator=gen) * 0.5).to(cuda)
+    t1 = theta.clone().requires_grad_(True)
+    d1 = [im.clone().requires_grad_(True) for im in ims]
+    outs = T.transform_data_mixed(d1, t1, outsizes)
+    flat = torch.cat([o.reshape(-1) for o in outs])
+    w = torch.randn(flat.shape, generator=gen).to(cuda)
+    (flat * w).sum().backward()
+    t2 = theta.clone().requires_grad_(True)
+    p2 = torch.cat([im.reshape(-1) for im in ims]).requires_grad_(True)
+    packed = T.transform_data_packed(p2, sizes, t2, outsizes)
+    assert torch.equal(packed, flat.detach())
+    (packed * w).sum().backward()
+    assert torch.equal(t1.grad, t2.grad)
+    assert _rel(torch.cat([d.grad.reshape(-1) for d in d1]), p2.grad) <= 1e-5
+
+
+@pytest.mark.gpu
 def test_mixed_layout_is_cached_and_theta_only(cuda):
     """Repeated calls with the same sizes reuse the device plan; theta without
     grad and images without grad run forward only."""
@@ -284,3 +309,22 @@ def test_mixed_argument_checks():
     T.params.integration = 'exact'
     with pytest.raises(ValueError, match='fixed-step'):
         F.transform_data_mixed([torch.zeros(1, 4, 4)] * 2, theta, T.params)
+
+
+def test_packed_argument_checks():
+    from libcpab_gb300 import functions as F
+    from libcpab_gb300.cpab import Cpab
+    T = Cpab([3, 3], backend='pytorch', device='gpu', zero_boundary=True)
+    theta = torch.zeros(2, T.get_theta_dim())
+    with pytest.raises(ValueError, match='theta'):
+        F.transform_data_packed(torch.zeros(32), [(4, 4)], theta, T.params)
+    with pytest.raises(ValueError, match='2 extents'):
+        F.transform_data_packed(torch.zeros(32), [(4, 4), (4,)], theta, T.params)
+    with pytest.raises(ValueError, match='1D'):
+        F.transform_data_packed(torch.zeros(2, 16), [(4, 4), (4, 4)], theta, T.params)
+    with pytest.raises(ValueError, match='pixels'):
+        F.transform_data_packed(torch.zeros(33), [(4, 4), (4, 4)], theta, T.params)
+    with pytest.raises(ValueError, match='CUDA'):
+        F.transform_data_packed(torch.zeros(64), [(4, 4), (4, 4)], theta, T.params)
+    assert F.transform_data_packed(torch.zeros(0), [], torch.zeros(0, T.get_theta_dim()),
+                                   T.params).numel() == 0
