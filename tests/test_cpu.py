@@ -9,7 +9,7 @@ import re
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, REPO, SMALL, load_golden
+from conftest import REPO, SMALL, load_golden
 
 NSTEPS = 50
 

@@ -13,7 +13,6 @@
 * alignment_by_gradient replayed as a CUDA graph follows the eager loop, and
   both reduce the loss.
 """
-import numpy as np
 import pytest
 import torch
 
