@@ -23,8 +23,12 @@
 //     sums S per cell and propagates lambda with the per-cell D = M - I;
 //     k_finalize applies G = h S (I + h/2 [A;0])^T + h^2/2 A_lin^T S once per
 //     cell.  The result is the reference's analytic gradient up to rounding.
-//     The trajectory is stepped with the equivalent single affine map
-//     p' = p + (h A~ + h^2/2 A~^2)[p;1] per cell (A~ = [A;0]; build_dtab).
+//     The forward sweep steps the trajectory with the reference's own
+//     operation order (ref_mid_step: float affine products, the h updates
+//     in emulated double), so its cells are the reference's; the reverse
+//     sweep rebuilds segment positions from those checkpoints with the
+//     equivalent single affine map p' = p + (h A~ + h^2/2 A~^2)[p;1] per
+//     cell (A~ = [A;0]; build_dtab, mid_map_step).
 //   mode 1 ("exact"): exact discrete adjoint of the forward map
 //     p' = p + E_c [p;1]:  dL/dT_c += lambda_{n+1} [p_n;1]^T,
 //     lambda_n = lambda_{n+1} + E_lin^T lambda_{n+1}; dL/dA then follows from

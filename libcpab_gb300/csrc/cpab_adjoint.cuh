@@ -7,67 +7,105 @@
 #include <tuple>
 
 #include "cpab_launch.h"
+#include "cpab_midpoint.cuh"
 
 namespace cpab {
 
 constexpr int kSeg = 10;
 
-struct Steps {
-    float h, hh, hh2;   // 1/N, 1/(2N), 1/(2N^2)
-};
+// Row stride of the per-cell adjoint table (16-byte aligned rows for the
+// vector loads in 2D and 3D): the N x N propagator D followed by N floats.
+template <int N>
+__host__ __device__ constexpr int dtab_stride() { return N == 1 ? 2 : (N == 2 ? 8 : 12); }
 
-inline Steps make_steps(int nsteps) {
-    Steps st;
-    st.h = (float)(1.0 / nsteps);
-    st.hh = (float)(0.5 / nsteps);
-    st.hh2 = (float)(0.5 / ((double)nsteps * nsteps));
-    return st;
-}
-
-// One forward step of the trajectory that the adjoint differentiates,
-// p += M [p; 1] with the cell's map from the table: E in mode 1 (the
-// compensated step of k_integrate), the midpoint-rule step map in mode 0
-// (build_dtab turns A into it).
-template <int N, int MODE>
-__device__ __forceinline__ void traj_step(const float *tab, int c, const Steps &st,
-                                          float (&p)[N]) {
-    constexpr int P = N * (N + 1);
-    float M[P], y[N];
-    load_cell<N>(tab, c, M);
-    affine_apply<N>(M, p, y);
+// The midpoint step of an affine field is itself affine,
+// p + h A~(p~ + h/2 A~ p~) = p + (h A~ + h^2/2 A~^2) p~ (A~ = [A; 0]): one map
+// per cell.  The reverse sweep rebuilds segment positions with it (from the
+// exactly stepped checkpoints of the forward sweep: positions within a few
+// ulp of the reference's, which only the sums of lambda p~^T see).
+template <int N>
+__device__ __forceinline__ void mid_map_step(const float *dtab, int c, float (&p)[N]) {
+    const float *src = dtab + c * dtab_stride<N>();
+    float D[N * N], m[N];
+    if constexpr (N == 1) {
+        const float2 a = *reinterpret_cast<const float2 *>(src);
+        D[0] = a.x; m[0] = a.y;
+    } else if constexpr (N == 2) {
+        const float4 a = *reinterpret_cast<const float4 *>(src);
+        const float2 b = *reinterpret_cast<const float2 *>(src + 4);
+        D[0] = a.x; D[1] = a.y; D[2] = a.z; D[3] = a.w; m[0] = b.x; m[1] = b.y;
+    } else {
+        const float4 a = reinterpret_cast<const float4 *>(src)[0];
+        const float4 b = reinterpret_cast<const float4 *>(src)[1];
+        const float4 d = reinterpret_cast<const float4 *>(src)[2];
+        D[0] = a.x; D[1] = a.y; D[2] = a.z; D[3] = a.w;
+        D[4] = b.x; D[5] = b.y; D[6] = b.z; D[7] = b.w;
+        D[8] = d.x; m[0] = d.y; m[1] = d.z; m[2] = d.w;
+    }
+    float y[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+        float acc = m[r];
+#pragma unroll
+        for (int k = 0; k < N; ++k) acc = fmaf(D[r * N + k], p[k], acc);
+        y[r] = acc;
+    }
 #pragma unroll
     for (int r = 0; r < N; ++r) p[r] += y[r];
 }
 
-// Row stride of the per-cell adjoint propagator table (16-byte aligned rows
-// for the vector loads).
-template <int N>
-__host__ __device__ constexpr int dtab_stride() { return N == 1 ? 1 : (N == 2 ? 4 : 12); }
-
-// Per-cell propagator of the adjoint, D with lambda_n = lambda_{n+1} + D^T lambda_{n+1}:
-//   mode 0: D = h A_lin + h^2/2 A_lin^2  (M - I of the midpoint sensitivity)
-//   mode 1: D = E_lin                     (the linear part of T - I)
-// stored row-major, D[r][k] at dtab[c * stride + r * N + k].
-// In mode 0 the cell table is then turned, in place, from A into the step
-// map of the midpoint rule, which for an affine field is itself affine:
-// p + h A~(p~ + h/2 A~ p~) = p + (h A~ + h^2/2 A~^2) p~ (A~ = [A; 0]), so
-// traj_step applies one map per step (its linear part is D).  Cells are split
-// over the calling threads (first, first + stride, ...); the caller
-// synchronises.
+// One forward step of the trajectory that the adjoint differentiates: the
+// reference's midpoint rule in mode 0 (tab holds A), the compensated step
+// p += E [p; 1] of k_integrate in mode 1 (tab holds E).
 template <int N, int MODE>
-__device__ __forceinline__ void build_dtab(float *tab, float *dtab, int nC, const Steps &st,
+__device__ __forceinline__ void traj_step(const float *tab, int c, const Steps &st,
+                                          float (&p)[N]) {
+    if constexpr (MODE == 0) {
+        float A[N * (N + 1)];
+        load_cell<N>(tab, c, A);
+        ref_mid_step<N>(A, st, p);
+    } else {
+        constexpr int P = N * (N + 1);
+        float M[P], y[N];
+        load_cell<N>(tab, c, M);
+        affine_apply<N>(M, p, y);
+#pragma unroll
+        for (int r = 0; r < N; ++r) p[r] += y[r];
+    }
+}
+
+// The step the reverse sweep uses to rebuild a segment from its checkpoint:
+// the midpoint map from dtab in mode 0, the compensated step in mode 1.
+template <int N, int MODE>
+__device__ __forceinline__ void rebuild_step(const float *tab, const float *dtab, int c,
+                                             const Steps &st, float (&p)[N]) {
+    if constexpr (MODE == 0) mid_map_step<N>(dtab, c, p);
+    else traj_step<N, 1>(tab, c, st, p);
+}
+
+// Per-cell adjoint table, row c at dtab[c * dtab_stride<N>()]:
+//   D (N x N, row-major) with lambda_n = lambda_{n+1} + D^T lambda_{n+1}:
+//     mode 0: D = h A_lin + h^2/2 A_lin^2  (M - I of the midpoint sensitivity)
+//     mode 1: D = E_lin                     (the linear part of T - I)
+//   then N floats: mode 0, the translation of the midpoint map
+//     (h a + h^2/2 A_lin a, a = the cell's translation column; mid_map_step);
+//     mode 1, zeros.
+// tab keeps A (mode 0) or E (mode 1).  Cells are split over the calling
+// threads (first, first + stride, ...); the caller synchronises.
+template <int N, int MODE>
+__device__ __forceinline__ void build_dtab(const float *tab, float *dtab, int nC, const Steps &st,
                                            int first, int stride) {
-    constexpr int P = N * (N + 1);
     for (int c = first; c < nC; c += stride) {
-        float *a = tab + c * P;
+        const float *a = tab + c * (N * (N + 1));
         float *d = dtab + c * dtab_stride<N>();
         if constexpr (MODE == 1) {
 #pragma unroll
-            for (int r = 0; r < N; ++r)
+            for (int r = 0; r < N; ++r) {
 #pragma unroll
                 for (int k = 0; k < N; ++k) d[r * N + k] = a[r * (N + 1) + k];
+                d[N * N + r] = 0.f;
+            }
         } else {
-            float m2[P];
 #pragma unroll
             for (int r = 0; r < N; ++r)
 #pragma unroll
@@ -75,14 +113,10 @@ __device__ __forceinline__ void build_dtab(float *tab, float *dtab, int nC, cons
                     float s = 0.f;
 #pragma unroll
                     for (int m = 0; m < N; ++m) s = fmaf(a[r * (N + 1) + m], a[m * (N + 1) + k], s);
-                    m2[r * (N + 1) + k] = fmaf(st.h, a[r * (N + 1) + k], st.hh2 * s);
+                    const float v = fmaf(st.h, a[r * (N + 1) + k], st.hh2 * s);
+                    if (k < N) d[r * N + k] = v;
+                    else d[N * N + r] = v;
                 }
-#pragma unroll
-            for (int r = 0; r < N; ++r)
-#pragma unroll
-                for (int k = 0; k < N; ++k) d[r * N + k] = m2[r * (N + 1) + k];
-#pragma unroll
-            for (int i = 0; i < P; ++i) a[i] = m2[i];
         }
     }
 }
@@ -406,7 +440,7 @@ __device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nste
         for (int s = 0; s < len; ++s) {
 #pragma unroll
             for (int r = 0; r < N; ++r) sm.pb[(s * N + r) * B + tid] = x[r];
-            traj_step<N, MODE>(sm.tab, (int)sm.cl[(n0 + s) * B + tid], st, x);
+            rebuild_step<N, MODE>(sm.tab, sm.dtab, (int)sm.cl[(n0 + s) * B + tid], st, x);
         }
 #pragma unroll 1
         for (int s = len - 1; s >= 0; --s) {

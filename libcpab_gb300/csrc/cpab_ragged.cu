@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256)
 template <int MODE>
 __host__ __device__ inline int ragged_warp_floats(int nC) {
     const int Gr = round4(nC * 2);
-    return Gr * (MODE == 0 ? 2 : 1) + round4(nC) + Gr;
+    return Gr * (MODE == 0 ? 2 : 1) + round4(nC * dtab_stride<1>()) + Gr;
 }
 
 template <int MODE, typename CT>
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(256)
     sm.tab = mine;
     float *tabE = (MODE == 0) ? mine + Gr : mine;
     sm.dtab = mine + Gr * (MODE == 0 ? 2 : 1);
-    sm.gw = sm.dtab + round4(t.nC);
+    sm.gw = sm.dtab + round4(t.nC * dtab_stride<1>());
     sm.ck = base_f + (size_t)W * ragged_warp_floats<MODE>(t.nC);
     sm.pb = sm.ck + (size_t)nseg * B;
     sm.cl = reinterpret_cast<CT *>(sm.pb + (size_t)kSeg * B);

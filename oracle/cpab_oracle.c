@@ -243,6 +243,34 @@ void oracle_backward(int ndim, const int *nc, int nsteps, const float *points, i
     }
 }
 
+/*
+ * The midpoint trajectory that cpab_backward_op differentiates
+ * (libcpab/core/cpab_ops.cpp:300-366: v = A[p;1], pMid = p + h v / 2 with h a
+ * double, vMid = A[pMid;1], p += vMid * h) for the points [ndim, nP] of one
+ * theta with cell table As [nC, ndim, ndim+1].  out [ndim, nP] receives the
+ * end points, cells [nP, nsteps] the cell of every step.
+ */
+void oracle_midpoint_trajectory(int ndim, const int *nc, int nsteps, const float *points,
+                                long nP, const float *As, float *out, int *cells) {
+    const int ppc = ndim * (ndim + 1);
+    const double h = 1.0 / nsteps;
+    #pragma omp parallel for schedule(static)
+    for (long i = 0; i < nP; i++) {
+        float p[3], v[3], pm[3], vm[3];
+        for (int j = 0; j < ndim; j++) p[j] = points[i + j * nP];
+        for (int s = 0; s < nsteps; s++) {
+            const int c = oracle_cell(ndim, p, nc);
+            cells[i * nsteps + s] = c;
+            const float *A = As + (long)c * ppc;
+            affine(ndim, v, A, p);
+            for (int j = 0; j < ndim; j++) pm[j] = (float)(p[j] + h * v[j] / 2.0);
+            affine(ndim, vm, A, pm);
+            for (int j = 0; j < ndim; j++) p[j] = (float)(p[j] + vm[j] * h);
+        }
+        for (int j = 0; j < ndim; j++) out[i + j * nP] = p[j];
+    }
+}
+
 /* ---------------- interpolation (libcpab/pytorch/interpolation.py) ---------------- */
 
 static long clampl(long v, long lo, long hi) { return v < lo ? lo : (v > hi ? hi : v); }

@@ -67,6 +67,8 @@ class Oracle:
                                          _f32p, _i32p, _f32p]
         L.oracle_interpolate_backward.argtypes = [ctypes.c_int, _f32p, ctypes.c_int, ctypes.c_int,
                                                   _i32p, _f32p, _i32p, _f32p, _f64p, _f32p]
+        L.oracle_midpoint_trajectory.argtypes = [ctypes.c_int, _i32p, ctypes.c_int, _f32p,
+                                                 ctypes.c_long, _f32p, _f32p, _i32p]
         L.oracle_num_threads.restype = ctypes.c_int
         L.oracle_set_threads.argtypes = [ctypes.c_int]
 
@@ -114,6 +116,20 @@ class Oracle:
                                  _p(A, _f32p), n_theta, _p(B, _f32p), d, _p(g, _f32p),
                                  _p(out, _f64p))
         return out
+
+    def midpoint_trajectory(self, nc, nsteps, points, As):
+        """The reference's midpoint trajectory of points [ndim, nP] under one
+        theta's cell table As [nC, ndim, ndim+1]: (end points [ndim, nP],
+        cells [nP, nsteps])."""
+        pts = np.ascontiguousarray(points, dtype=np.float32)
+        A = np.ascontiguousarray(As, dtype=np.float32)
+        ndim, nP = pts.shape
+        nca = np.asarray(nc, dtype=np.int32)
+        out = np.empty((ndim, nP), dtype=np.float32)
+        cells = np.empty((nP, nsteps), dtype=np.int32)
+        self.lib.oracle_midpoint_trajectory(ndim, _p(nca, _i32p), nsteps, _p(pts, _f32p), nP,
+                                            _p(A, _f32p), _p(out, _f32p), _p(cells, _i32p))
+        return out, cells
 
     def interpolate(self, data, grid, outsize):
         D = np.ascontiguousarray(data, dtype=np.float32)
@@ -180,6 +196,63 @@ class RefLib:
         self.lib.ref_forward(_p(out, _f32p), _p(pts, _f32p), _p(tr, _f32p), _p(ns, _i32p),
                              _p(nca, _i32p), ndim, nP, n_theta, broadcast)
         return out
+
+    def _chunks(self, n_theta, nP, threads):
+        per = max(256, -(-nP * n_theta // (4 * threads)))
+        return [(t, a, min(nP, a + per)) for t in range(n_theta) for a in range(0, nP, per)]
+
+    def forward_threaded(self, nc, nsteps, points, trels, threads):
+        """ref_forward over (theta, point-chunk) slices on `threads` host
+        threads (the op itself is single-threaded); points [ndim, nP]."""
+        import concurrent.futures
+        pts = np.ascontiguousarray(points, dtype=np.float32)
+        tr = np.ascontiguousarray(trels, dtype=np.float32)
+        n_theta, (ndim, nP) = tr.shape[0], pts.shape
+        nca = np.asarray(nc, dtype=np.int32)
+        ns = np.asarray([nsteps], dtype=np.int32)
+        out = np.zeros((n_theta, ndim, nP), dtype=np.float32)
+
+        def run(job):
+            t, a, b = job
+            sub = np.ascontiguousarray(pts[:, a:b])
+            o = np.zeros((1, ndim, b - a), dtype=np.float32)
+            self.lib.ref_forward(_p(o, _f32p), _p(sub, _f32p), _p(tr[t], _f32p), _p(ns, _i32p),
+                                 _p(nca, _i32p), ndim, b - a, 1, 0)
+            out[t, :, a:b] = o[0]
+        with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(run, self._chunks(n_theta, nP, threads)))
+        return out
+
+    def dtheta_threaded(self, nc, nsteps, points, As, Bs, grad, threads):
+        """The reference's analytic gradient, dtheta [n_theta, d]: ref_backward
+        (the [d, 1, ndim, chunk] sensitivity of one theta's point chunk)
+        contracted with grad [n_theta, ndim, nP] (float64 sums), over
+        (theta, point-chunk) slices on `threads` host threads."""
+        import concurrent.futures
+        pts = np.ascontiguousarray(points, dtype=np.float32)
+        A = np.ascontiguousarray(As, dtype=np.float32)
+        B = np.ascontiguousarray(Bs, dtype=np.float32)
+        n_theta, nC = A.shape[0], A.shape[1]
+        d = B.shape[0]
+        ndim, nP = pts.shape
+        nca = np.asarray(nc, dtype=np.int32)
+        ns = np.asarray([nsteps], dtype=np.int32)
+        jobs = self._chunks(n_theta, nP, threads)
+
+        def run(job):
+            t, a, b = job
+            sub = np.ascontiguousarray(pts[:, a:b])
+            sens = np.zeros((d, 1, ndim, b - a), dtype=np.float32)
+            self.lib.ref_backward(_p(sens, _f32p), _p(sub, _f32p), _p(A[t], _f32p),
+                                  _p(B, _f32p), _p(ns, _i32p), _p(nca, _i32p), 1, d, ndim,
+                                  b - a, nC, 0)
+            return t, np.einsum('kjp,jp->k', sens[:, 0].astype(np.float64),
+                                grad[t, :, a:b].astype(np.float64))
+        dth = np.zeros((n_theta, d))
+        with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+            for t, part in ex.map(run, jobs):
+                dth[t] += part
+        return dth
 
     def backward_sensitivity(self, nc, nsteps, points, As, Bs):
         """The reference's [d, n_theta, ndim, nP] sensitivity tensor."""
