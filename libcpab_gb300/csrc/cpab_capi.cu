@@ -7,6 +7,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
+
 #include "../../include/cpab_gb300.h"
 #include "cpab_interp.cuh"
 #include "cpab_launch.h"
@@ -31,19 +33,31 @@ int cuda_fail(cudaError_t e, const char *what) {
 
 // Device error word, one per device (file-scope __device__ variable; its
 // device address is looked up once per device).
+// The per-device address caches are filled by whichever host thread calls
+// first; relaxed atomics make the concurrent fills (all of the same value)
+// well defined.
 __device__ unsigned g_device_error;
 constexpr int kMaxDevices = 64;
-unsigned *g_err_ptr[kMaxDevices] = {nullptr};
+std::atomic<unsigned *> g_err_ptr[kMaxDevices];
 
 unsigned *device_error_word() {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
-    if (!g_err_ptr[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_device_error) != cudaSuccess) return nullptr;
-        g_err_ptr[dev] = static_cast<unsigned *>(p);
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();   // leave no error behind for the next launch check
+        return nullptr;
     }
-    return g_err_ptr[dev];
+    if (dev < 0 || dev >= kMaxDevices) return nullptr;
+    unsigned *w = g_err_ptr[dev].load(std::memory_order_relaxed);
+    if (!w) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_device_error) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        w = static_cast<unsigned *>(p);
+        g_err_ptr[dev].store(w, std::memory_order_relaxed);
+    }
+    return w;
 }
 
 // Validate a tessellation and fill its constants (tess_init).
@@ -213,6 +227,7 @@ int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *po
     if (mode == CPAB_GRAD_EXACT && !E) return fail(CPAB_ERR_ARGUMENT, "exact mode needs E");
     cudaStream_t s = as_stream(stream);
     if (nP == 0) {
+        if (d == 0) return CPAB_OK;
         cudaError_t e = cudaMemsetAsync(dtheta, 0, (size_t)n_theta * d * sizeof(float), s);
         return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "memset");
     }
@@ -955,12 +970,13 @@ namespace {
 
 constexpr size_t kNoAllocScratchFloats = size_t(1) << 21;
 __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];
-float *g_noalloc_ptr[kMaxDevices] = {nullptr};
+std::atomic<float *> g_noalloc_ptr[kMaxDevices];
 
 float *noalloc_scratch(int *rc) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) {
+        cudaGetLastError();
         *rc = cuda_fail(e, "cudaGetDevice");
         return nullptr;
     }
@@ -968,17 +984,23 @@ float *noalloc_scratch(int *rc) {
         *rc = fail(CPAB_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
         return nullptr;
     }
-    if (!g_noalloc_ptr[dev]) {
-        float *ptr = nullptr;
+    float *ptr = g_noalloc_ptr[dev].load(std::memory_order_relaxed);
+    if (!ptr) {
         e = cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess || !ptr) {
+        if (e != cudaSuccess) {
+            cudaGetLastError();   // the failure is reported here, not by the next launch
             *rc = cuda_fail(e, "cudaGetSymbolAddress of the no-alloc scratch");
             return nullptr;
         }
-        g_noalloc_ptr[dev] = ptr;
+        if (!ptr) {
+            *rc = fail(CPAB_ERR_CUDA, "cudaGetSymbolAddress of the no-alloc scratch gave no "
+                                      "address");
+            return nullptr;
+        }
+        g_noalloc_ptr[dev].store(ptr, std::memory_order_relaxed);
     }
     *rc = CPAB_OK;
-    return g_noalloc_ptr[dev];
+    return ptr;
 }
 
 }  // namespace
@@ -1005,6 +1027,7 @@ int cpab_backward_noalloc(int ndim, const int *nc, int nsteps, int mode, const f
     if (mode == CPAB_GRAD_EXACT && !E) return fail(CPAB_ERR_ARGUMENT, "exact mode needs E");
     cudaStream_t s = as_stream(stream);
     if (nP == 0) {
+        if (d == 0) return CPAB_OK;
         cudaError_t e = cudaMemsetAsync(dtheta, 0, (size_t)n_theta * d * sizeof(float), s);
         return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "memset");
     }

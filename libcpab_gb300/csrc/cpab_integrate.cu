@@ -14,6 +14,8 @@
 //   * compensated update p <- p + E [p;1] with E = T - I (or the reference's
 //     p <- T [p;1] when handed the reference's T tables);
 //   * structure-of-arrays point I/O, coalesced along the point index.
+#include <atomic>
+
 #include "cpab_launch.h"
 
 namespace cpab {
@@ -134,15 +136,27 @@ cudaError_t launch_findcellidx(const Tess &t, const float *points, long long nP,
     return cudaGetLastError();
 }
 
+// SM count of the current device, looked up once per device (relaxed atomics:
+// concurrent first calls store the same value).
 int num_sms() {
-    static int cached = 0;
-    if (cached == 0) {
-        int dev = 0, n = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        cached = n > 0 ? n : 148;
+    constexpr int kDevices = 64;
+    static std::atomic<int> cached[kDevices];
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        dev = 0;
     }
-    return cached;
+    if (dev < 0 || dev >= kDevices) dev = 0;
+    int v = cached[dev].load(std::memory_order_relaxed);
+    if (v == 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            n = 0;
+        }
+        v = n > 0 ? n : 152;
+        cached[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
 }
 
 }  // namespace cpab

@@ -40,12 +40,17 @@ def _inputs(cuda, name='2d_3x3_zb', mode=0):
 
 
 def _noalloc(N, nc, mode, pts, A, E, basis, cot, want_dpoints=True):
+    """pts: [n_theta, ndim, nP] (one point set per theta) or [ndim, nP]
+    (shared by all theta); dpoints come back [n_theta, ndim, nP] either way."""
     ndim = len(nc)
     n_theta, d = A.shape[0], basis.shape[1]
+    broadcast = int(pts.dim() == 3)
+    nP = pts.shape[-1]
     dtheta = torch.full((n_theta, d), float('nan'), device=pts.device)
-    dpoints = torch.full(pts.shape, float('nan'), device=pts.device) if want_dpoints else None
+    dpoints = torch.full((n_theta, ndim, nP), float('nan'), device=pts.device) \
+        if want_dpoints else None
     rc = N.load().cpab_backward_noalloc(
-        ndim, N._ints(nc), NSTEPS, mode, _ptr(pts), 1, pts.shape[-1], _ptr(A), _ptr(E), n_theta,
+        ndim, N._ints(nc), NSTEPS, mode, _ptr(pts), broadcast, nP, _ptr(A), _ptr(E), n_theta,
         _ptr(basis), d, _ptr(cot), _ptr(dtheta), _ptr(dpoints), None,
         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     return rc, dtheta, dpoints
@@ -91,6 +96,34 @@ def test_noalloc_3d_and_large_batch(cuda):
         rc, dth, _ = _noalloc(N, [8, 8], 0, pts, A, E, basis, cot, want_dpoints=False)
         assert rc == 0, N.load().cpab_last_error()
         assert _rel(dth, ref_dth) <= 1e-5
+
+
+@pytest.mark.parametrize('mode', [0, 1])
+def test_noalloc_capped_blocks_shared_points(mode, cuda):
+    """Points shared by all theta ([ndim, nP]), dpoints wanted, on a problem
+    where the fixed scratch holds one CTA slice per theta while cpab_backward
+    plans more: 1D with 4,096 cells (8,192 floats per theta), 200 theta.  The
+    tables come from a random basis (the kernels do not need a CPAB basis)."""
+    from libcpab_gb300 import _native as N
+    nc, n_theta, nP, d = [4096], 200, 3000, 6
+    gen = torch.Generator(device=cuda).manual_seed(5)
+    basis = 0.3 * torch.randn(4096 * 2, d, device=cuda, generator=gen)
+    theta = torch.randn(n_theta, d, device=cuda, generator=gen)
+    A, _, E = N.cell_tables(nc, NSTEPS, theta, basis)
+    pts = torch.rand(1, nP, device=cuda, generator=gen)
+    cot = torch.randn(n_theta, 1, nP, device=cuda, generator=gen)
+    slice_bytes = n_theta * 4096 * 2 * 4
+    assert (1 << 21) * 4 < 2 * slice_bytes                # one slice per theta fits
+    ws = N.load().cpab_backward_workspace(1, N._ints(nc), NSTEPS, nP, n_theta)
+    assert ws >= 2 * slice_bytes                          # cpab_backward: >= 2 CTAs per theta
+    ref_dth, ref_dp = N.backward(nc, NSTEPS, mode, pts, A, E, basis, cot, want_dpoints=True)
+    for _ in range(2):
+        rc, dth, dp = _noalloc(N, nc, mode, pts, A, E, basis, cot)
+        assert rc == 0, N.load().cpab_last_error()
+        torch.cuda.synchronize()
+        assert torch.equal(dp, ref_dp)
+        assert _rel(dth, ref_dth) <= 1e-5
+    assert N.device_status() == 0
 
 
 @pytest.mark.parametrize('mode', [0, 1])
