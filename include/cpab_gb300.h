@@ -44,9 +44,16 @@ extern "C" {
 #define CPAB_ERR_UNSUPPORTED 3  /* configuration beyond a kernel's limits */
 #define CPAB_ERR_WORKSPACE 4    /* workspace missing or too small         */
 
-/* Gradient modes of cpab_backward / cpab_transform_data_backward. */
-#define CPAB_GRAD_REFERENCE 0   /* the reference's midpoint-rule analytic gradient */
+/* Gradient modes of cpab_backward / cpab_transform_data_backward (and of the
+ * ragged and no-alloc backward entry points). */
+#define CPAB_GRAD_REFERENCE 0   /* the reference's midpoint-rule analytic gradient,
+                                   along the reference's own midpoint trajectory  */
 #define CPAB_GRAD_EXACT 1       /* exact derivative of the forward map             */
+#define CPAB_GRAD_REFERENCE_MAP 2 /* the reference's gradient formula along the
+                                   trajectory of the per-cell midpoint map (one
+                                   affine map per step, fewer instructions); its
+                                   cells can differ from the reference's where a
+                                   step lands within rounding of a cell boundary */
 
 /* Bits reported by cpab_device_status. */
 #define CPAB_DEV_TMA_TIMEOUT 1u /* a bulk copy to shared memory did not complete */
@@ -117,8 +124,11 @@ CPAB_API size_t cpab_backward_workspace(int ndim, const int *nc, int nsteps, lon
  * dL/dtheta [n_theta, d] (and optionally dL/dpoints [n_theta, ndim, nP]) from
  * grad_out = dL/d(out) [n_theta, ndim, nP].
  *   mode CPAB_GRAD_REFERENCE: the reference's analytic gradient (midpoint-rule
- *     sensitivity, libcpab/core/cpab_ops.cu:390-697) computed in reverse mode;
- *     needs A.
+ *     sensitivity, libcpab/core/cpab_ops.cu:390-697) computed in reverse mode
+ *     along the reference's midpoint trajectory in its own arithmetic
+ *     (libcpab/core/cpab_ops.cpp:306-365); needs A.
+ *   mode CPAB_GRAD_REFERENCE_MAP: the same gradient along the trajectory of
+ *     the collapsed per-cell midpoint map; needs A.
  *   mode CPAB_GRAD_EXACT: exact adjoint of cpab_integrate; needs A and E.
  * Replaces cpab_gpu.backward (libcpab/pytorch/transformer_cuda.cpp:43-70) and
  * the contraction gradient.mul_(grad).sum(dim=(2,3))
@@ -213,8 +223,8 @@ CPAB_API size_t cpab_transform_data_backward_workspace(int ndim, const int *nc, 
 /*
  * Fused transform_data backward from grad_out = dL/d(out) (image layout):
  * ddata (overwritten, may be NULL) and dtheta [nb, d].  Mode
- * CPAB_GRAD_REFERENCE needs A and grid_saved (from cpab_transform_data);
- * CPAB_GRAD_EXACT needs A and E.
+ * CPAB_GRAD_REFERENCE and CPAB_GRAD_REFERENCE_MAP need A and grid_saved (from
+ * cpab_transform_data); CPAB_GRAD_EXACT needs A and E.
  */
 CPAB_API int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, int mode,
                                  const float *lin, const int *outsize, const float *A,
@@ -388,7 +398,7 @@ CPAB_API int cpab_ragged_points_forward(int ndim, const int *nc, int nsteps, con
  * Backward of cpab_ragged_points_forward from grad_out = dL/d(out)
  * [ndim, total]: dtheta [S, d] (overwritten; deterministic) and dpoints
  * [ndim, total] (overwritten, may be NULL).  Mode as in cpab_backward
- * (CPAB_GRAD_REFERENCE needs A; CPAB_GRAD_EXACT needs A and E).
+ * (CPAB_GRAD_REFERENCE and CPAB_GRAD_REFERENCE_MAP need A; CPAB_GRAD_EXACT needs A and E).
  */
 CPAB_API int cpab_ragged_points_backward(int ndim, const int *nc, int nsteps, int mode,
                                          const float *A, const float *E, int S,

@@ -11,10 +11,14 @@ TransformGridRagged -- transformer for many point sets of uneven sizes, one
                   theta per set, in one persistent launch
 
 Gradient modes (params.gradient):
-  'reference' -- the reference's analytic gradient: the midpoint-rule
-                 sensitivity of libcpab/core/cpab_ops.cu:390-697, evaluated in
-                 reverse mode (default, for drop-in parity);
-  'exact'     -- the exact derivative of the forward map that was evaluated.
+  'reference'     -- the reference's analytic gradient: the midpoint-rule
+                     sensitivity of libcpab/core/cpab_ops.cu:390-697, evaluated
+                     in reverse mode along the reference's own midpoint
+                     trajectory (default, for drop-in parity);
+  'reference_map' -- the same gradient along the trajectory of the collapsed
+                     per-cell midpoint map (fewer instructions per step; its
+                     cells can differ from the reference's at boundary ties);
+  'exact'         -- the exact derivative of the forward map that was evaluated.
 """
 from __future__ import annotations
 
@@ -24,11 +28,15 @@ from torch.autograd.function import once_differentiable
 from . import _native as N
 
 
+_MODES = {'reference': N.GRAD_REFERENCE, 'exact': N.GRAD_EXACT,
+          'reference_map': N.GRAD_REFERENCE_MAP}
+
+
 def _mode(params):
     g = getattr(params, 'gradient', 'reference')
-    if g not in ('reference', 'exact'):
-        raise ValueError("params.gradient must be 'reference' or 'exact' (got %r)" % (g,))
-    return N.GRAD_EXACT if g == 'exact' else N.GRAD_REFERENCE
+    if g not in _MODES:
+        raise ValueError("params.gradient must be one of %s (got %r)" % (sorted(_MODES), g))
+    return _MODES[g]
 
 
 def _ties(params):
@@ -154,7 +162,7 @@ class TransformData(torch.autograd.Function):
         data_c = data.detach().to(torch.float32).contiguous()
         mode = _mode(params)
         needs_grad = ctx.needs_input_grad[0] or ctx.needs_input_grad[1]
-        save_grid = needs_grad and mode == N.GRAD_REFERENCE
+        save_grid = needs_grad and mode != N.GRAD_EXACT
         if staged is None:
             theta_c = theta.detach().to(torch.float32).contiguous()
             dev = data.device

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, 'libcpab_gb300.so')
 
 GRAD_REFERENCE = 0
 GRAD_EXACT = 1
+GRAD_REFERENCE_MAP = 2
 
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _vp = ctypes.c_void_p
@@ -546,7 +547,7 @@ def sequential_transform_data_backward(ncs, nsteps, mode, lin, outsize, Es, A_la
     for t, name in ((lin, 'lin'), (A_last, 'A_last'), (data, 'data'), (basis_last, 'basis_last'),
                     (grad_out, 'grad_out')):
         _require(t, name)
-    if mode == GRAD_REFERENCE:
+    if mode != GRAD_EXACT:
         _require(grid_saved, 'grid_saved')
     nb, C = data.shape[0], data.shape[1]
     d = basis_last.shape[1]

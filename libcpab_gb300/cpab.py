@@ -109,9 +109,12 @@ class Cpab(object):
 
         use_slow selected the reference's pure-PyTorch loop; the same
         fixed-step scheme always runs in the CUDA kernels here, so it only
-        records the flag.  gradient ('reference' or 'exact') selects the
-        backward: the reference's analytic (midpoint-rule sensitivity)
-        gradient, or the exact derivative of the forward map.
+        records the flag.  gradient selects the backward: 'reference' (the
+        reference's analytic midpoint-rule sensitivity gradient along its own
+        midpoint trajectory), 'reference_map' (the same gradient along the
+        trajectory of the collapsed per-cell midpoint map: faster, with cells
+        that can differ from the reference's at boundary ties) or 'exact' (the
+        exact derivative of the forward map).
         point_gradient (default False, as the reference, whose
         transform_grid returns no gradient for the points:
         libcpab/pytorch/transformer.py:202) makes transform_grid also
@@ -126,7 +129,8 @@ class Cpab(object):
         assert type(numeric_grad) == bool, 'numeric_grad must be bool'
         assert type(use_slow) == bool, 'use_slow must be bool'
         if gradient is not None:
-            assert gradient in ('reference', 'exact'), "gradient must be 'reference' or 'exact'"
+            assert gradient in ('reference', 'reference_map', 'exact'), \
+                "gradient must be 'reference', 'reference_map' or 'exact'"
             self.params.gradient = gradient
         if integration is not None:
             assert integration in ('fixed_step', 'exact'), \

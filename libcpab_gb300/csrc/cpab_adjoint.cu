@@ -127,7 +127,7 @@ static bool plan_adjoint_mode_uncached(const Tess &t, int nsteps, int mode, long
                                        int n_theta, AdjointPlan *plan, bool allow_global) {
     const bool small = t.nC <= 256;
 #define CPAB_PLAN(N)                                                                          \
-    if (mode == 0)                                                                            \
+    if (mode != 1)                                                                            \
         return small ? plan_t<N, 0, uint8_t>(t, nsteps, nP, n_theta, plan, allow_global)      \
                      : plan_t<N, 0, uint16_t>(t, nsteps, nP, n_theta, plan, allow_global);    \
     return small ? plan_t<N, 1, uint8_t>(t, nsteps, nP, n_theta, plan, allow_global)          \
@@ -193,6 +193,13 @@ cudaError_t launch_adjoint(const Tess &t, int nsteps, int mode, const AdjointPla
                      : launch_adjoint_t<N, 0, uint16_t>(t, nsteps, plan, points, broadcast, nP, \
                                                         table, n_theta, gout, dpoints,          \
                                                         partials, ties, err, s);                \
+    if (mode == 2)                                                                              \
+        return small ? launch_adjoint_t<N, 2, uint8_t>(t, nsteps, plan, points, broadcast, nP,  \
+                                                       table, n_theta, gout, dpoints, partials, \
+                                                       ties, err, s)                            \
+                     : launch_adjoint_t<N, 2, uint16_t>(t, nsteps, plan, points, broadcast, nP, \
+                                                        table, n_theta, gout, dpoints,          \
+                                                        partials, ties, err, s);                \
     return small ? launch_adjoint_t<N, 1, uint8_t>(t, nsteps, plan, points, broadcast, nP,      \
                                                    table, n_theta, gout, dpoints, partials,     \
                                                    ties, err, s)                                \
@@ -256,7 +263,7 @@ cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *pa
         kern<<<n_theta, block, smem, s>>>(t.nC, st, partials, parts, A, basis, d, dtheta);     \
         return cudaGetLastError();                                                             \
     }
-    if (mode == 0) {
+    if (mode != 1) {   // modes 0 and 2: the midpoint sensitivity's cell map
         switch (t.ndim) {
             case 1: CPAB_FIN(1, 0)
             case 2: CPAB_FIN(2, 0)

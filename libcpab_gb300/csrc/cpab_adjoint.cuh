@@ -13,10 +13,25 @@ namespace cpab {
 
 constexpr int kSeg = 10;
 
-// Row stride of the per-cell adjoint table (16-byte aligned rows for the
-// vector loads in 2D and 3D): the N x N propagator D followed by N floats.
+// The per-cell adjoint table (build_dtab) is two arrays: the N x N
+// propagators D (row stride dtab_stride, 16-byte aligned rows for the vector
+// loads in 2D and 3D), then the N-float translations of the midpoint maps
+// (row stride mtab_stride) starting at mtab_of.
 template <int N>
-__host__ __device__ constexpr int dtab_stride() { return N == 1 ? 2 : (N == 2 ? 8 : 12); }
+__host__ __device__ constexpr int dtab_stride() { return N == 1 ? 1 : (N == 2 ? 4 : 12); }
+template <int N>
+__host__ __device__ constexpr int mtab_stride() { return N == 1 ? 1 : (N == 2 ? 2 : 4); }
+
+__host__ __device__ inline int round4(int x) { return (x + 3) & ~3; }
+
+template <int N>
+__host__ __device__ inline int dtab_floats(int nC) {
+    return round4(nC * dtab_stride<N>()) + round4(nC * mtab_stride<N>());
+}
+template <int N>
+__host__ __device__ inline float *mtab_of(float *dtab, int nC) {
+    return dtab + round4(nC * dtab_stride<N>());
+}
 
 // The midpoint step of an affine field is itself affine,
 // p + h A~(p~ + h/2 A~ p~) = p + (h A~ + h^2/2 A~^2) p~ (A~ = [A; 0]): one map
@@ -24,23 +39,22 @@ __host__ __device__ constexpr int dtab_stride() { return N == 1 ? 2 : (N == 2 ? 
 // exactly stepped checkpoints of the forward sweep: positions within a few
 // ulp of the reference's, which only the sums of lambda p~^T see).
 template <int N>
-__device__ __forceinline__ void mid_map_step(const float *dtab, int c, float (&p)[N]) {
-    const float *src = dtab + c * dtab_stride<N>();
+__device__ __forceinline__ void load_dtab(const float *dtab, int c, float (&D)[N * N]);
+
+template <int N>
+__device__ __forceinline__ void mid_map_step(const float *dtab, const float *mtab, int c,
+                                             float (&p)[N]) {
     float D[N * N], m[N];
+    load_dtab<N>(dtab, c, D);
+    const float *ms = mtab + c * mtab_stride<N>();
     if constexpr (N == 1) {
-        const float2 a = *reinterpret_cast<const float2 *>(src);
-        D[0] = a.x; m[0] = a.y;
+        m[0] = ms[0];
     } else if constexpr (N == 2) {
-        const float4 a = *reinterpret_cast<const float4 *>(src);
-        const float2 b = *reinterpret_cast<const float2 *>(src + 4);
-        D[0] = a.x; D[1] = a.y; D[2] = a.z; D[3] = a.w; m[0] = b.x; m[1] = b.y;
+        const float2 b = *reinterpret_cast<const float2 *>(ms);
+        m[0] = b.x; m[1] = b.y;
     } else {
-        const float4 a = reinterpret_cast<const float4 *>(src)[0];
-        const float4 b = reinterpret_cast<const float4 *>(src)[1];
-        const float4 d = reinterpret_cast<const float4 *>(src)[2];
-        D[0] = a.x; D[1] = a.y; D[2] = a.z; D[3] = a.w;
-        D[4] = b.x; D[5] = b.y; D[6] = b.z; D[7] = b.w;
-        D[8] = d.x; m[0] = d.y; m[1] = d.z; m[2] = d.w;
+        const float4 b = *reinterpret_cast<const float4 *>(ms);
+        m[0] = b.x; m[1] = b.y; m[2] = b.z;
     }
     float y[N];
 #pragma unroll
@@ -55,8 +69,9 @@ __device__ __forceinline__ void mid_map_step(const float *dtab, int c, float (&p
 }
 
 // One forward step of the trajectory that the adjoint differentiates: the
-// reference's midpoint rule in mode 0 (tab holds A), the compensated step
-// p += E [p; 1] of k_integrate in mode 1 (tab holds E).
+// reference's midpoint rule in modes 0 and 2 (tab holds A), the compensated
+// step p += E [p; 1] of k_integrate in mode 1 (tab holds E).  Mode 2's
+// logged forward takes the collapsed midpoint map instead (forward_step).
 template <int N, int MODE>
 __device__ __forceinline__ void traj_step(const float *tab, int c, const Steps &st,
                                           float (&p)[N]) {
@@ -77,34 +92,34 @@ __device__ __forceinline__ void traj_step(const float *tab, int c, const Steps &
 // The step the reverse sweep uses to rebuild a segment from its checkpoint:
 // the midpoint map from dtab in mode 0, the compensated step in mode 1.
 template <int N, int MODE>
-__device__ __forceinline__ void rebuild_step(const float *tab, const float *dtab, int c,
-                                             const Steps &st, float (&p)[N]) {
-    if constexpr (MODE == 0) mid_map_step<N>(dtab, c, p);
+__device__ __forceinline__ void rebuild_step(const float *tab, const float *dtab,
+                                             const float *mtab, int c, const Steps &st,
+                                             float (&p)[N]) {
+    if constexpr (MODE != 1) mid_map_step<N>(dtab, mtab, c, p);
     else traj_step<N, 1>(tab, c, st, p);
 }
 
-// Per-cell adjoint table, row c at dtab[c * dtab_stride<N>()]:
-//   D (N x N, row-major) with lambda_n = lambda_{n+1} + D^T lambda_{n+1}:
-//     mode 0: D = h A_lin + h^2/2 A_lin^2  (M - I of the midpoint sensitivity)
-//     mode 1: D = E_lin                     (the linear part of T - I)
-//   then N floats: mode 0, the translation of the midpoint map
-//     (h a + h^2/2 A_lin a, a = the cell's translation column; mid_map_step);
-//     mode 1, zeros.
-// tab keeps A (mode 0) or E (mode 1).  Cells are split over the calling
-// threads (first, first + stride, ...); the caller synchronises.
+// Per-cell adjoint table: row c of D at dtab[c * dtab_stride<N>()], the N x N
+// propagator (row-major) with lambda_n = lambda_{n+1} + D^T lambda_{n+1}:
+//     modes 0, 2: D = h A_lin + h^2/2 A_lin^2  (M - I of the midpoint sensitivity)
+//     mode 1:     D = E_lin                     (the linear part of T - I)
+// and, in modes 0 and 2, row c of mtab = mtab_of(dtab, nC), the translation of the
+// midpoint map h a + h^2/2 A_lin a (a = the cell's translation column;
+// mid_map_step).  tab keeps A (modes 0, 2) or E (mode 1).  Cells are split over
+// the calling threads (first, first + stride, ...); the caller synchronises.
 template <int N, int MODE>
 __device__ __forceinline__ void build_dtab(const float *tab, float *dtab, int nC, const Steps &st,
                                            int first, int stride) {
+    float *mtab = mtab_of<N>(dtab, nC);
     for (int c = first; c < nC; c += stride) {
         const float *a = tab + c * (N * (N + 1));
         float *d = dtab + c * dtab_stride<N>();
+        float *m = mtab + c * mtab_stride<N>();
         if constexpr (MODE == 1) {
 #pragma unroll
-            for (int r = 0; r < N; ++r) {
+            for (int r = 0; r < N; ++r)
 #pragma unroll
                 for (int k = 0; k < N; ++k) d[r * N + k] = a[r * (N + 1) + k];
-                d[N * N + r] = 0.f;
-            }
         } else {
 #pragma unroll
             for (int r = 0; r < N; ++r)
@@ -112,11 +127,12 @@ __device__ __forceinline__ void build_dtab(const float *tab, float *dtab, int nC
                 for (int k = 0; k <= N; ++k) {
                     float s = 0.f;
 #pragma unroll
-                    for (int m = 0; m < N; ++m) s = fmaf(a[r * (N + 1) + m], a[m * (N + 1) + k], s);
+                    for (int q = 0; q < N; ++q) s = fmaf(a[r * (N + 1) + q], a[q * (N + 1) + k], s);
                     const float v = fmaf(st.h, a[r * (N + 1) + k], st.hh2 * s);
                     if (k < N) d[r * N + k] = v;
-                    else d[N * N + r] = v;
+                    else m[r] = v;
                 }
+            if constexpr (N == 3) m[3] = 0.f;
         }
     }
 }
@@ -164,11 +180,9 @@ __device__ __forceinline__ void adjoint_step(const float *dtab, int c, const flo
     for (int k = 0; k < N; ++k) lam[k] = nl[k];
 }
 
-__host__ __device__ inline int round4(int x) { return (x + 3) & ~3; }
-
 // Shared memory carve-up for the adjoint kernels (floats unless noted):
 //   tab   [round4(G)]            cell table of this theta (TMA destination)
-//   dtab  [round4(nC*stride)]    per-cell adjoint propagators D
+//   dtab  [dtab_floats(nC)]      per-cell propagators D and midpoint-map translations
 //   gw    [W][round4(G)]         per-warp cell-gradient tables (or in global memory, see
 //                                carve_adjoint)
 //   ck    [nseg][N][block]       checkpoints (position every kSeg steps)
@@ -181,7 +195,7 @@ __host__ __device__ inline size_t adjoint_smem_bytes(int nC, int nsteps, int blo
                                                      bool gw_in_smem = true) {
     constexpr int P = N * (N + 1);
     const int G = round4(nC * P);
-    const int Dn = round4(nC * dtab_stride<N>());
+    const int Dn = dtab_floats<N>(nC);
     const int W = gw_in_smem ? block / 32 : 0;
     const int nseg = (nsteps + kSeg - 1) / kSeg;
     size_t b = (size_t)G * 4 + (size_t)Dn * 4 + (size_t)W * G * 4 +
@@ -259,7 +273,7 @@ struct PlanCache {
 
 template <int N, typename CT>
 struct AdjSmem {
-    float *tab, *dtab, *gw, *ck, *pb;
+    float *tab, *dtab, *mtab, *gw, *ck, *pb;
     CT *cl;
 };
 
@@ -277,7 +291,8 @@ __device__ __forceinline__ AdjSmem<N, CT> carve_adjoint(float *base, int nC, int
     AdjSmem<N, CT> s;
     s.tab = base;
     s.dtab = s.tab + Gr;
-    float *after = s.dtab + round4(nC * dtab_stride<N>());
+    s.mtab = mtab_of<N>(s.dtab, nC);
+    float *after = s.dtab + dtab_floats<N>(nC);
     if constexpr (GWG) {   // a template choice keeps the shared-memory path's
         s.gw = gw_ext;     // flushes on shared-memory instructions
         s.ck = after;
@@ -440,7 +455,8 @@ __device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nste
         for (int s = 0; s < len; ++s) {
 #pragma unroll
             for (int r = 0; r < N; ++r) sm.pb[(s * N + r) * B + tid] = x[r];
-            rebuild_step<N, MODE>(sm.tab, sm.dtab, (int)sm.cl[(n0 + s) * B + tid], st, x);
+            rebuild_step<N, MODE>(sm.tab, sm.dtab, sm.mtab, (int)sm.cl[(n0 + s) * B + tid], st,
+                                  x);
         }
 #pragma unroll 1
         for (int s = len - 1; s >= 0; --s) {
@@ -493,7 +509,8 @@ __device__ __forceinline__ void logged_forward(const AdjSmem<N, CT> &sm, const T
         for (int n = n0; n < end; ++n) {
             int c = find_cell<N>(p, t, ties);
             sm.cl[n * B + tid] = (CT)c;
-            traj_step<N, MODE>(sm.tab, c, st, p);
+            if constexpr (MODE == 2) mid_map_step<N>(sm.dtab, sm.mtab, c, p);
+            else traj_step<N, MODE>(sm.tab, c, st, p);
         }
     }
 }
@@ -615,7 +632,7 @@ __device__ __forceinline__ void finish_theta(float *g, float *red, const float *
                                              float *__restrict__ dth) {
     constexpr int P = N * (N + 1);
     const int tid = threadIdx.x, B = blockDim.x, G = nC * P;
-    if constexpr (MODE == 0) {
+    if constexpr (MODE != 1) {
         // S_c = sum_n lambda_{n+1} [p_n;1]^T  ->
         // G_c = h S_c (I + h/2 [A_c;0])^T + h^2/2 A_lin^T S_c
         for (int c = tid; c < nC; c += B) {

@@ -27,6 +27,11 @@ int fail(int code, const char *fmt, ...) {
     return code;
 }
 
+bool grad_mode_ok(int mode) {
+    return mode == CPAB_GRAD_REFERENCE || mode == CPAB_GRAD_EXACT ||
+           mode == CPAB_GRAD_REFERENCE_MAP;
+}
+
 int cuda_fail(cudaError_t e, const char *what) {
     return fail(CPAB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
@@ -217,7 +222,7 @@ int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *po
     int rc = make_tess(ndim, nc, &t);
     if (rc) return rc;
     if ((rc = check_steps(nsteps))) return rc;
-    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+    if (!grad_mode_ok(mode))
         return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
     if (nP < 0 || n_theta < 0 || d < 0) return fail(CPAB_ERR_ARGUMENT, "invalid sizes");
     if ((rc = check_theta_count(n_theta))) return rc;
@@ -447,7 +452,7 @@ size_t cpab_transform_data_backward_workspace(int ndim, const int *nc, int nstep
     Tess t;
     if (make_tess(ndim, nc, &t) || check_steps(nsteps) || check_sizes(ndim, outsize, "outsize"))
         return 0;
-    if (nb <= 0 || (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)) return 0;
+    if (nb <= 0 || (!grad_mode_ok(mode))) return 0;
     long long nP = 1;
     for (int j = 0; j < ndim; ++j) nP *= outsize[j];
     AdjointPlan plan;
@@ -475,14 +480,14 @@ static int td_backward(int ndim, const int *nc, int nsteps, int mode, const floa
     if ((rc = check_steps(nsteps))) return rc;
     if ((rc = check_geo(ndim, size, outsize, nb)))
         return rc;
-    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+    if (!grad_mode_ok(mode))
         return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
     if (nb < 0 || C < 1 || d < 0) return fail(CPAB_ERR_ARGUMENT, "invalid nb, C or d");
     if (nb == 0) return CPAB_OK;
     if (!lin || !A || !data || !grad_out || (d > 0 && (!basis || !dtheta)))
         return fail(CPAB_ERR_ARGUMENT, "lin, A, data, basis, grad_out or dtheta is NULL");
     if (mode == CPAB_GRAD_EXACT && !E) return fail(CPAB_ERR_ARGUMENT, "exact mode needs E");
-    if (mode == CPAB_GRAD_REFERENCE && !grid_saved)
+    if (mode != CPAB_GRAD_EXACT && !grid_saved)
         return fail(CPAB_ERR_ARGUMENT, "reference mode needs grid_saved");
     long long nP = 1;
     for (int j = 0; j < ndim; ++j) nP *= outsize[j];
@@ -724,7 +729,7 @@ int cpab_ragged1d_backward(int nc, int nsteps, int mode, const float *A, const f
     Tess t;
     int rc = check_ragged(nc, nsteps, S, total, offsets, &t);
     if (rc) return rc;
-    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+    if (!grad_mode_ok(mode))
         return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
     if (d < 0) return fail(CPAB_ERR_ARGUMENT, "negative d");
     if (S == 0) return CPAB_OK;
@@ -753,7 +758,7 @@ int cpab_ragged1d_mse(int nc, int nsteps, int mode, const float *A, const float 
     Tess t;
     int rc = check_ragged(nc, nsteps, S, total, offsets, &t);
     if (rc) return rc;
-    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+    if (!grad_mode_ok(mode))
         return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
     if (d < 0) return fail(CPAB_ERR_ARGUMENT, "negative d");
     if (S == 0) return CPAB_OK;
@@ -786,7 +791,7 @@ int cpab_ragged1d_tune(int kind, int nc, int nsteps, int mode, const float *A, c
     if (rc) return rc;
     if (kind != kRaggedForward && kind != kRaggedAdjoint)
         return fail(CPAB_ERR_ARGUMENT, "kind must be 0 (forward) or 1 (adjoint)");
-    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+    if (!grad_mode_ok(mode))
         return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
     if (S == 0 || total == 0) return fail(CPAB_ERR_ARGUMENT, "nothing to tune (no points)");
     if (!E || !values || !out || (kind == kRaggedAdjoint &&
@@ -916,7 +921,7 @@ int cpab_ragged_points_backward(int ndim, const int *nc, int nsteps, int mode, c
     int rc = check_ragged_points(ndim, nc, nsteps, S, total, offsets, workspace,
                                  workspace_bytes, &t);
     if (rc) return rc;
-    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+    if (!grad_mode_ok(mode))
         return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
     if (d < 0) return fail(CPAB_ERR_ARGUMENT, "negative d");
     if (S == 0) return CPAB_OK;
@@ -1017,7 +1022,7 @@ int cpab_backward_noalloc(int ndim, const int *nc, int nsteps, int mode, const f
     int rc = make_tess(ndim, nc, &t);
     if (rc) return rc;
     if ((rc = check_steps(nsteps))) return rc;
-    if (mode != CPAB_GRAD_REFERENCE && mode != CPAB_GRAD_EXACT)
+    if (!grad_mode_ok(mode))
         return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
     if (nP < 0 || n_theta < 0 || d < 0) return fail(CPAB_ERR_ARGUMENT, "invalid sizes");
     if ((rc = check_theta_count(n_theta))) return rc;

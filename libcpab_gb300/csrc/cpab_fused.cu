@@ -252,7 +252,7 @@ static bool plan_td_uncached(const Tess &t, int nsteps, int mode, long long nP, 
                              AdjointPlan *plan) {
     const bool small = t.nC <= 256;
 #define CPAB_PLAN(N)                                                                          \
-    if (mode == 0)                                                                            \
+    if (mode != 1)                                                                            \
         return small ? plan_td_t<N, 0, uint8_t>(t, nsteps, nP, nb, plan)                      \
                      : plan_td_t<N, 0, uint16_t>(t, nsteps, nP, nb, plan);                    \
     return small ? plan_td_t<N, 1, uint8_t>(t, nsteps, nP, nb, plan)                          \
@@ -316,6 +316,13 @@ cudaError_t launch_transform_data_backward(const Tess &t, int nsteps, int mode,
                                                       grid_saved, nb, data, C, gout, ddata,     \
                                                       partials, ties, err, s)                   \
                      : launch_td_bwd_t<N, 0, uint16_t>(t, nsteps, plan, g, pre, lin, table,          \
+                                                       grid_saved, nb, data, C, gout, ddata,    \
+                                                       partials, ties, err, s);                 \
+    if (mode == 2)                                                                              \
+        return small ? launch_td_bwd_t<N, 2, uint8_t>(t, nsteps, plan, g, pre, lin, table,           \
+                                                      grid_saved, nb, data, C, gout, ddata,     \
+                                                      partials, ties, err, s)                   \
+                     : launch_td_bwd_t<N, 2, uint16_t>(t, nsteps, plan, g, pre, lin, table,          \
                                                        grid_saved, nb, data, C, gout, ddata,    \
                                                        partials, ties, err, s);                 \
     return small ? launch_td_bwd_t<N, 1, uint8_t>(t, nsteps, plan, g, pre, lin, table, grid_saved,   \

@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256)
 template <int MODE>
 __host__ __device__ inline int ragged_warp_floats(int nC) {
     const int Gr = round4(nC * 2);
-    return Gr * (MODE == 0 ? 2 : 1) + round4(nC * dtab_stride<1>()) + Gr;
+    return Gr * (MODE != 1 ? 2 : 1) + dtab_floats<1>(nC) + Gr;
 }
 
 template <int MODE, typename CT>
@@ -201,9 +201,10 @@ __global__ void __launch_bounds__(256)
     float *mine = base_f + (size_t)wib * ragged_warp_floats<MODE>(t.nC);
     AdjSmem<1, CT> sm;
     sm.tab = mine;
-    float *tabE = (MODE == 0) ? mine + Gr : mine;
-    sm.dtab = mine + Gr * (MODE == 0 ? 2 : 1);
-    sm.gw = sm.dtab + round4(t.nC * dtab_stride<1>());
+    float *tabE = (MODE != 1) ? mine + Gr : mine;
+    sm.dtab = mine + Gr * (MODE != 1 ? 2 : 1);
+    sm.mtab = mtab_of<1>(sm.dtab, t.nC);
+    sm.gw = sm.dtab + dtab_floats<1>(t.nC);
     sm.ck = base_f + (size_t)W * ragged_warp_floats<MODE>(t.nC);
     sm.pb = sm.ck + (size_t)nseg * B;
     sm.cl = reinterpret_cast<CT *>(sm.pb + (size_t)kSeg * B);
@@ -222,9 +223,9 @@ __global__ void __launch_bounds__(256)
 
     auto stage = [&](int sid) {
         __syncwarp();
-        const float *src = (MODE == 0 ? a.A : a.E) + (long long)sid * G;
+        const float *src = (MODE != 1 ? a.A : a.E) + (long long)sid * G;
         for (int i = lane; i < G; i += 32) sm.tab[i] = __ldg(src + i);
-        if (MODE == 0)
+        if (MODE != 1)
             for (int i = lane; i < G; i += 32) tabE[i] = __ldg(a.E + (long long)sid * G + i);
         for (int i = lane; i < Gr; i += 32) sm.gw[i] = 0.f;
         __syncwarp();
@@ -260,7 +261,7 @@ __global__ void __launch_bounds__(256)
             const bool live = j < L;
             float p[1] = {live ? linspace01(j, L, step) : 0.5f};
             float pN[1] = {p[0]};
-            if constexpr (MODE == 0) e_sweep<1>(tabE, t, nsteps, pN, ties, err);
+            if constexpr (MODE != 1) e_sweep<1>(tabE, t, nsteps, pN, ties, err);
             logged_forward<1, MODE, CT>(sm, t, nsteps, st, p, ties, err);
             if constexpr (MODE == 1) pN[0] = p[0];
             float lam[1] = {0.f};
@@ -407,7 +408,7 @@ static cudaError_t launch_ra_t(const Tess &t, int nsteps, int block, int ppt, in
 size_t ragged_adjoint_smem_for(const Tess &t, int nsteps, int mode, int block) {
     const bool small = t.nC <= 256;
     size_t b;
-    if (mode == 0)
+    if (mode != 1)
         b = small ? ragged_adjoint_smem<0, uint8_t>(t.nC, nsteps, block)
                   : ragged_adjoint_smem<0, uint16_t>(t.nC, nsteps, block);
     else
@@ -441,6 +442,10 @@ cudaError_t launch_ragged_adjoint(const Tess &t, int nsteps, int mode, bool fuse
     if (mode == 0) {
         if (small) { CPAB_RA(0, uint8_t) }
         CPAB_RA(0, uint16_t)
+    }
+    if (mode == 2) {
+        if (small) { CPAB_RA(2, uint8_t) }
+        CPAB_RA(2, uint16_t)
     }
     if (small) { CPAB_RA(1, uint8_t) }
     CPAB_RA(1, uint16_t)

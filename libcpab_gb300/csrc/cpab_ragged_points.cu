@@ -84,7 +84,7 @@ __global__ void __launch_bounds__(256)
 template <int N>
 __host__ __device__ inline int points_warp_floats(int nC) {
     const int Gr = round4(nC * N * (N + 1));
-    return 2 * Gr + round4(nC * dtab_stride<N>());
+    return 2 * Gr + dtab_floats<N>(nC);
 }
 
 template <int N, typename CT>
@@ -116,6 +116,7 @@ __global__ void __launch_bounds__(256, 3)
     sm.tab = mine;
     sm.gw = mine + Gr;
     sm.dtab = sm.gw + Gr;
+    sm.mtab = mtab_of<N>(sm.dtab, t.nC);
     sm.ck = base_f + (size_t)W * points_warp_floats<N>(t.nC);
     sm.pb = sm.ck + (size_t)nseg * N * B;
     sm.cl = reinterpret_cast<CT *>(sm.pb + (size_t)kSeg * N * B);
@@ -302,6 +303,13 @@ cudaError_t launch_ragged_points_backward(const Tess &t, int nsteps, int mode, i
                                                    points, gout, dpoints, partials, basis, d,  \
                                                    dtheta, ties, err, s)                       \
                      : launch_rpa_t<N, 0, uint16_t>(t, nsteps, S, off, tile_off, A, E, total,  \
+                                                    points, gout, dpoints, partials, basis, d, \
+                                                    dtheta, ties, err, s);                     \
+    if (mode == 2)                                                                             \
+        return small ? launch_rpa_t<N, 2, uint8_t>(t, nsteps, S, off, tile_off, A, E, total,   \
+                                                   points, gout, dpoints, partials, basis, d,  \
+                                                   dtheta, ties, err, s)                       \
+                     : launch_rpa_t<N, 2, uint16_t>(t, nsteps, S, off, tile_off, A, E, total,  \
                                                     points, gout, dpoints, partials, basis, d, \
                                                     dtheta, ties, err, s);                     \
     return small ? launch_rpa_t<N, 1, uint8_t>(t, nsteps, S, off, tile_off, A, E, total, points, \

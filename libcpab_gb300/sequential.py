@@ -46,7 +46,7 @@ class SequentialTransformData(torch.autograd.Function):
         needs = ctx.needs_input_grad[0] or ctx.needs_input_grad[-1]
         out, grid = N.sequential_transform_data(
             [p.nc for p in params_list], [p.nstepsolver for p in params_list], lin, outsize, Es,
-            data_c, save_grid=needs and mode == N.GRAD_REFERENCE, ties=_ties(last))
+            data_c, save_grid=needs and mode != N.GRAD_EXACT, ties=_ties(last))
         ctx.save_for_backward(data_c, lin, As[-1], grid, *Es)
         ctx.params_list = params_list
         ctx.outsize = outsize

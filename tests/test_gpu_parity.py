@@ -140,9 +140,10 @@ def test_transform_grid_vs_fp64(name, cuda):
 
 @pytest.mark.parametrize('name', SMALL)
 @pytest.mark.parametrize('which', ['grid', 'grid_b'])
-def test_gradient_reference_mode(name, which, cuda):
+@pytest.mark.parametrize('gradient', ['reference', 'reference_map'])
+def test_gradient_reference_mode(name, which, gradient, cuda):
     g = load_golden(name)
-    T = make_cpab(g, 'reference')
+    T = make_cpab(g, gradient)
     th = torch.tensor(g['theta'], device=cuda, requires_grad=True)
     out = T.transform_grid(torch.tensor(g[which], device=cuda), th)
     (out * torch.tensor(g['cot'], device=cuda)).sum().backward()
@@ -192,7 +193,7 @@ def test_points_get_no_gradient_by_default(cuda):
 def test_backward_deterministic(name, cuda):
     g = load_golden(name)
     res = []
-    for mode in ('reference', 'exact'):
+    for mode in ('reference', 'reference_map', 'exact'):
         T = make_cpab(g, mode)
         outs = []
         for _ in range(2):
@@ -220,7 +221,7 @@ def test_interpolate_vs_reference(name, cuda):
 
 
 @pytest.mark.parametrize('name', SMALL)
-@pytest.mark.parametrize('mode', ['reference', 'exact'])
+@pytest.mark.parametrize('mode', ['reference', 'reference_map', 'exact'])
 def test_transform_data_fused_matches_unfused(name, mode, cuda):
     """The fused kernel computes exactly transform_grid followed by
     interpolate; its gradients match the unfused chain."""

@@ -126,7 +126,7 @@ def test_ragged_forward_matches_per_series_path(small, oracle):
     assert N.device_status() == 0
 
 
-@pytest.mark.parametrize('mode', [0, 1])
+@pytest.mark.parametrize('mode', [0, 1, 2])
 def test_ragged_backward_matches_per_series_path(small, mode):
     P = small
     N = P['N']
@@ -168,7 +168,7 @@ def test_ragged_backward_matches_oracle_gradient(small, oracle):
         assert _rel(dth[s], torch.tensor(ref[0])) <= 1e-4, (s, _rel(dth[s], torch.tensor(ref[0])))
 
 
-@pytest.mark.parametrize('mode', [0, 1])
+@pytest.mark.parametrize('mode', [0, 1, 2])
 def test_ragged_mse_fused_matches_forward_backward(small, mode):
     P = small
     N = P['N']

@@ -84,7 +84,7 @@ def test_forward_matches_per_set_integrate(prob):
     assert N.device_status() == 0
 
 
-@pytest.mark.parametrize('mode', [0, 1])
+@pytest.mark.parametrize('mode', [0, 1, 2])
 def test_backward_matches_per_set_backward(prob, mode):
     P, N = prob, prob['N']
     gen = torch.Generator(device=P['pts'].device).manual_seed(11)

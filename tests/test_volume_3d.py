@@ -60,7 +60,7 @@ def test_volume_fused_forward_matches_unfused(volume):
     assert N.device_status() == 0
 
 
-@pytest.mark.parametrize('mode', [0, 1])
+@pytest.mark.parametrize('mode', [0, 1, 2])
 def test_volume_fused_backward_matches_unfused(volume, mode):
     V = volume
     N = V['N']

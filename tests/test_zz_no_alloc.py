@@ -61,7 +61,7 @@ def _rel(a, b):
     return float((a - b).abs().max() / b.abs().max().clamp_min(1e-30))
 
 
-@pytest.mark.parametrize('mode', [0, 1])
+@pytest.mark.parametrize('mode', [0, 1, 2])
 def test_noalloc_matches_workspace_backward_twice(mode, cuda):
     N, nc, pts, A, E, basis, cot = _inputs(cuda)
     ref_dth, ref_dpts = N.backward(nc, NSTEPS, mode, pts, A, E, basis, cot, want_dpoints=True)
@@ -98,7 +98,7 @@ def test_noalloc_3d_and_large_batch(cuda):
         assert _rel(dth, ref_dth) <= 1e-5
 
 
-@pytest.mark.parametrize('mode', [0, 1])
+@pytest.mark.parametrize('mode', [0, 1, 2])
 def test_noalloc_capped_blocks_shared_points(mode, cuda):
     """Points shared by all theta ([ndim, nP]), dpoints wanted, on a problem
     where the fixed scratch holds one CTA slice per theta while cpab_backward
@@ -126,7 +126,7 @@ def test_noalloc_capped_blocks_shared_points(mode, cuda):
     assert N.device_status() == 0
 
 
-@pytest.mark.parametrize('mode', [0, 1])
+@pytest.mark.parametrize('mode', [0, 1, 2])
 def test_3d_global_warp_tables_match_shared(mode, cuda):
     """3D [4,4,4] (320 cells): cpab_backward keeps its per-warp gradient tables
     in the workspace (more warps per SM); the no-alloc entry point keeps them
