@@ -54,18 +54,20 @@ def parse():
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=5)
     ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
-    ap.add_argument('--cpu-sample-images', type=int, default=1)
+    ap.add_argument('--cpu-sample-images', type=int, default=CPU_SAMPLE_IMAGES)
     ap.add_argument('--batch', type=int, default=BATCH,
                     help='images per step (the headline workload uses 64; smaller values '
                          'are for profiling runs only)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--leg', default='all',
                     choices=['all', 'ragged', 'volume', 'interp', 'aligner', 'exact', 'points',
-                             'mixed'],
+                             'mixed', 'plain'],
                     help='run only one of the side workloads and print its result (for '
                          'profiling runs)')
     ap.add_argument('--no-tune', action='store_true',
                     help='ragged leg: use the default launch shapes instead of autotuning')
+    ap.add_argument('--no-plain', action='store_true',
+                    help="skip the reference's own GPU path (the plain comparator)")
     ap.add_argument('--no-extra', action='store_true',
                     help='skip the workloads reported beside the headline (ragged 1D '
                          'series, 3D volume warp, interpolator sweep)')
@@ -294,14 +296,19 @@ def run_gb300(args):
     lin = torch.cat([torch.linspace(0, 1, SIZE, device=device)] * 2).contiguous()
     out, grid = N.transform_data(NC, NSTEPS, lin, [SIZE, SIZE], E, data, save_grid=True)
     gout = (2.0 / out.numel()) * (out - target)
-    ws_need = N.load().cpab_transform_data_backward_workspace(2, N._ints(NC), NSTEPS, 0,
-                                                               N._ints([SIZE, SIZE]), args.batch)
+    ws_need = max(N.load().cpab_transform_data_backward_workspace(
+        2, N._ints(NC), NSTEPS, m, N._ints([SIZE, SIZE]), args.batch) for m in (0, 1, 2))
     ws = torch.empty(ws_need, dtype=torch.uint8, device=device)
     t_fwd = time_events(lambda: N.transform_data(NC, NSTEPS, lin, [SIZE, SIZE], E, data,
                                                  save_grid=True), args.steps, flush)
     t_bwd = time_events(lambda: N.transform_data_backward(NC, NSTEPS, 0, lin, [SIZE, SIZE], A, E,
                                                           grid, data, basis, gout,
                                                           workspace=ws), args.steps, flush)
+    # the other gradient modes' fused backward on the same inputs
+    t_bwd_modes = {name: time_events(
+        lambda m=m: N.transform_data_backward(NC, NSTEPS, m, lin, [SIZE, SIZE], A, E, grid, data,
+                                              basis, gout, workspace=ws), args.steps, flush)
+        for name, m in (('reference_map', 2), ('exact', 1))}
     # the plain one-kernel-per-op GPU path through the same public API:
     # uniform_meshgrid -> transform_grid -> interpolate (libcpab/cpab.py:304-331
     # unfused), with the same loss and gradients
@@ -325,6 +332,49 @@ def run_gb300(args):
     exact = run_exact_flow(device, args.steps, flush) if extra else None
     points = run_ragged_points(device, args.steps, flush) if extra else None
     mixed = run_mixed_images(device, args.steps, flush) if extra else None
+    # results of the timed inputs on the first images, for the check against
+    # the FP64 oracle and the reference's gradient (run on the host after
+    # the GPU work): traced trajectories, warped images, dtheta, d(data)
+    check = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        n = max(1, min(args.cpu_sample_images, args.batch))
+        out_t, cells_t = N.integrate_trace(NC, NSTEPS, mesh, E[:n].contiguous())
+        check = {'out': out_t.cpu().numpy(), 'cells': cells_t.cpu().numpy(),
+                 'image': out[:n].cpu().numpy(), 'dtheta': e_dth[:n].cpu().numpy(),
+                 'ddata': e_dd[:n].cpu().numpy(), 'inputs': (theta_h, data_h, target_h)}
+    # the reference's own GPU path on the same inputs (the metric's "plain
+    # GPU"), last: it runs code that is not this library's
+    plain = None
+    if rank == 0 and not args.no_plain:
+        plain = run_plain_gpu_reference(device, theta, data, target, flush)
+        if '_result' in plain:
+            p_loss, p_dth, p_dd, p_grid, p_out = plain.pop('_result')
+            # this library's fused backward fed the reference's own warped grid
+            # and output (its fp32 step maps T put points up to ~1e-5 from this
+            # library's, across bilinear pixel knots where the interpolation
+            # gradient jumps): what is left is the gradient arithmetic
+            try:
+                p_gout = (2.0 / p_out.numel()) * (p_out - target)
+                o_dd, o_dth = N.transform_data_backward(NC, NSTEPS, 0, lin, [SIZE, SIZE], A, E,
+                                                        p_grid, data, basis, p_gout,
+                                                        workspace=ws)
+                plain['dtheta_rel_diff_on_reference_grid'] = float(
+                    (p_dth - o_dth).abs().max() / p_dth.abs().max())
+                plain['ddata_rel_diff_on_reference_grid'] = float(
+                    (p_dd - o_dd).abs().max() / p_dd.abs().max())
+                plain['grid_max_abs_diff_vs_this_library'] = float((p_grid - grid).abs().max())
+            except Exception as e:    # report, do not fail the bench
+                plain['decomposition_error'] = '%s: %s' % (type(e).__name__, str(e)[:200])
+            plain['eager_fused_speedup'] = plain['ms_per_step'] / ms_eager
+            plain['headline_speedup'] = plain['ms_per_step'] / ms_step
+            plain['target_speedup'] = 5.0
+            plain['dtheta_rel_diff_vs_this_library'] = float(
+                (p_dth - e_dth).abs().max() / e_dth.abs().max())
+            plain['ddata_rel_diff_vs_this_library'] = float(
+                (p_dd - e_dd).abs().max() / e_dd.abs().max())
+            plain['loss_rel_diff_vs_this_library'] = float(abs(p_loss - e_loss) / abs(e_loss))
+            del p_loss, p_dth, p_dd, p_grid, p_out
+        torch.cuda.empty_cache()
     clk = clocks.stop() if clocks else None
     status = N.device_status()
 
@@ -388,6 +438,13 @@ def run_gb300(args):
                 'source': 'instructions per point-step from ncu (%d bwd, %d fwd); peak = '
                           '152 SMs x 4 schedulers x 1 instruction/cycle at the sampled SM '
                           'clock' % (INSTR_BWD_STEP, INSTR_FWD_STEP)},
+            'backward_ms_per_launch_by_gradient_mode': {
+                'reference': bwd_ms,
+                **{k: sum(v) / len(v) for k, v in t_bwd_modes.items()},
+                'note': "k_transform_data_backward + k_finalize; 'reference' (the default and "
+                        "the headline) follows the reference's midpoint trajectory in its own "
+                        "arithmetic, 'reference_map' the collapsed per-cell midpoint map, "
+                        "'exact' is the exact adjoint of the forward map"},
             'forward_kernel': {'name': 'k_transform_data', 'ms_per_launch': fwd_ms,
                                'flop_per_launch': pts * NSTEPS * FLOP_FWD_STEP,
                                'tflops': pts * NSTEPS * FLOP_FWD_STEP / (fwd_ms / 1e3) / 1e12,
@@ -398,6 +455,7 @@ def run_gb300(args):
                             'ms_per_step': sum(t_unf) / len(t_unf),
                             'value': pts / (sum(t_unf) / len(t_unf) / 1e3),
                             'unit': 'points/s'},
+            'plain_gpu_reference': plain,
             'ragged_1d': ragged,
             'volume_3d': volume,
             'interpolate_2d': interp,
@@ -406,6 +464,7 @@ def run_gb300(args):
             'ragged_points_2d': points,
             'mixed_size_images_2d': mixed,
             'clocks': clk, 'device_status': status,
+            '_check': check,
         }
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -624,6 +683,68 @@ def run_mixed_images(device, steps, flush):
     return res
 
 
+PLAIN_STEPS = 3
+
+
+def run_plain_gpu_reference(device, theta, data, target, flush, steps=PLAIN_STEPS):
+    """The headline step through the reference's own pytorch GPU path, run
+    unmodified from baseline/_ref (baseline/plain_gpu.py): Cpab.transform_data
+    (basis upload, Pade expm with its host sync, the cpab_gpu forward kernel,
+    gather interpolation), F.mse_loss and autograd (the cpab_gpu analytic
+    backward writing the [d, n_theta, 2, nP] sensitivity tensor, its
+    contraction, the interpolation's scatter backward).  Same inputs, eager,
+    L2 flushed before each timed step.  Returns a dict, or one with
+    'unavailable' when the reference op is not built."""
+    try:
+        from baseline import plain_gpu
+        from libcpab_gb300.tessellation import make_tessellation
+        ref = plain_gpu.load()
+        # override: the reference builds its basis here, with this machine's
+        # LAPACK, as this library does (a null-space basis from an SVD is
+        # only defined up to rotation, so a basis file from another machine
+        # would give theta another meaning)
+        T = ref.Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True, override=True)
+        basis_diff = float(np.abs(T.params.basis - make_tessellation(NC, True, False).B).max())
+
+        def step():
+            th = theta.detach().requires_grad_(True)
+            dd = data.detach().requires_grad_(True)
+            out = T.transform_data(dd, th, [SIZE, SIZE])
+            loss = F.mse_loss(out, target)
+            loss.backward()
+            return loss.detach(), th.grad, dd.grad
+        loss, dth, dd = step()
+        with torch.no_grad():   # its warped grid and output, for the decomposition
+            mesh = T.uniform_meshgrid([SIZE, SIZE])
+            ref_grid = T.transform_grid(mesh, theta).contiguous()
+            ref_out = T.interpolate(data, ref_grid, [SIZE, SIZE]).contiguous()
+        torch.cuda.synchronize()
+        t = time_events(step, steps, flush)
+    except Exception as e:    # the comparator is optional: report, do not fail the bench
+        return {'unavailable': '%s: %s' % (type(e).__name__, str(e)[:300])}
+    ms = statistics.median(t)
+    pts = theta.shape[0] * SIZE * SIZE
+    return {'path': "reference libcpab, unmodified (baseline/_ref): Cpab.transform_data "
+                    "(backend='pytorch', device='gpu') + F.mse_loss + backward; its CUDA op "
+                    "JIT-built for sm_103a by its own torch.utils.cpp_extension.load",
+            'ms_per_step': ms, 'ms_all': t, 'value': pts / (ms / 1e3), 'unit': 'points/s',
+            'steps': steps, 'chunking': 'none: its [34, 64, 2, 50176] sensitivity tensor '
+                                        '(873 MB) fits',
+            'basis_max_abs_diff_vs_this_library': basis_diff,
+            '_result': (loss, dth, dd, ref_grid, ref_out)}
+
+
+def run_plain_leg(device, steps, flush):
+    """The plain comparator alone on the headline inputs (for profiling runs)."""
+    from libcpab_gb300 import Cpab
+    T = Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True)
+    theta, data, target = make_inputs(T, device)
+    res = run_plain_gpu_reference(device, theta.to(device), data.to(device),
+                                  target.to(device), flush, steps=max(1, steps))
+    res.pop('_result', None)
+    return res
+
+
 def hbm_peak():
     """Measured copy bandwidth of this GPU model (GB/s), else the fallback."""
     try:
@@ -775,67 +896,142 @@ def run_exact_flow(device, steps, flush):
             'max_abs_diff_exact_vs_fixed_step': float((ex - fs).abs().max())}
 
 
-def cpu_reference_step(sample, orc, T_h, nc):
-    """The reference's CPU implementation of one step on a sample of images:
-    forward op + interpolation, interpolation backward, analytic-gradient
-    backward op (oracle/cpab_oracle.c restates libcpab/core/cpab_ops.cpp and
-    libcpab/pytorch/interpolation.py)."""
-    theta, data, target, grid, As, Bs = sample
-    out_grid = orc.forward(nc, NSTEPS, grid, T_h)
-    out = orc.interpolate(data, out_grid, [SIZE, SIZE])
-    gout = (2.0 * (out - target) / out.size).astype(np.float32)
-    ddata, dgrid = orc.interpolate_backward(data, out_grid, [SIZE, SIZE], gout)
-    dtheta = orc.backward(nc, NSTEPS, grid, As, Bs, dgrid)
+CPU_SAMPLE_IMAGES, CPU_STEPS = 4, 3
+
+
+def cpu_sample(n_img, given=None):
+    """The headline inputs of the first n_img images on the host, plus the
+    tables the reference's CPU op takes.  `given` = (theta, data, target) of
+    the GPU run; otherwise they are rebuilt with the same seeds, the target
+    being the images warped by the second theta (reference step maps and
+    interpolation through the oracle; not timed)."""
+    from oracle.oracle import Oracle, step_maps_fp64
+    from libcpab_gb300.tessellation import make_tessellation
+    basis = make_tessellation(NC, True, False).B
+    d = basis.shape[1]
+    lin = np.linspace(0, 1, SIZE, dtype=np.float32)
+    gx, gy = np.meshgrid(lin, lin, indexing='xy')
+    grid = np.ascontiguousarray(np.stack([gx.reshape(-1), gy.reshape(-1)]), dtype=np.float32)
+
+    def tables(th):
+        Tm = step_maps_fp64(basis, th, 2, NSTEPS)[:, :, :2, :].astype(np.float32)
+        As = (basis @ th.astype(np.float64).T).T.reshape(th.shape[0], -1, 2, 3).astype(np.float32)
+        return Tm, As
+    if given is not None:
+        th, data, target = (np.ascontiguousarray(x[:n_img].numpy()) for x in given)
+    else:
+        th = (THETA_STD * torch.randn(BATCH, d, generator=torch.Generator().manual_seed(0)))
+        th = th[:n_img].numpy()
+        raw = torch.rand(BATCH, CHANNELS, SIZE, SIZE, generator=torch.Generator().manual_seed(1))
+        data = F.avg_pool2d(raw, kernel_size=5, stride=1, padding=2, count_include_pad=False)
+        data = np.ascontiguousarray(data[:n_img].numpy())
+        th2 = THETA_STD * torch.randn(BATCH, d, generator=torch.Generator().manual_seed(2))
+        T2, _ = tables(th2[:n_img].numpy())
+        orc = Oracle()
+        target = orc.interpolate(data, orc.forward(NC, NSTEPS, grid, T2), [SIZE, SIZE])
+    Tm, As = tables(th)
+    Bs = basis.T.reshape(d, -1, 2, 3).astype(np.float32)
+    return {'theta': th, 'data': data, 'target': np.ascontiguousarray(target, dtype=np.float32),
+            'grid': grid, 'T': Tm, 'A': As, 'B': Bs, 'basis': basis,
+            'n_total': BATCH * CHANNELS * SIZE * SIZE}
+
+
+def cpu_reference_step(s, orc, ref, threads):
+    """One step of the reference's CPU path on the sample: the integration
+    forward, the interpolation, its backward, the analytic-gradient backward
+    and its contraction.  The integration ops are the reference's own
+    libcpab/core/cpab_ops.cpp (oracle/_ref, run on `threads` host threads
+    over (theta, point-chunk) slices) when it is built, else their C
+    restatement; the interpolation is the C restatement of
+    libcpab/pytorch/interpolation.py (OpenMP)."""
+    if ref is not None:
+        out_grid = ref.forward_threaded(NC, NSTEPS, s['grid'], s['T'], threads)
+    else:
+        out_grid = orc.forward(NC, NSTEPS, s['grid'], s['T'])
+    out = orc.interpolate(s['data'], out_grid, [SIZE, SIZE])
+    gout = (2.0 * (out - s['target']) / s['n_total']).astype(np.float32)
+    ddata, dgrid = orc.interpolate_backward(s['data'], out_grid, [SIZE, SIZE], gout)
+    if ref is not None:
+        dtheta = ref.dtheta_threaded(NC, NSTEPS, s['grid'], s['A'], s['B'], dgrid, threads)
+    else:
+        dtheta = orc.backward(NC, NSTEPS, s['grid'], s['A'], s['B'], dgrid)
     return dtheta, ddata
 
 
-def cpu_sample(T, n_img):
-    from oracle.oracle import step_maps_fp64
-    theta, data, target = make_inputs_cpu(T)
-    th = theta[:n_img].numpy()
-    basis = T.params.basis
-    Tm = step_maps_fp64(basis, th, 2, NSTEPS)[:, :, :2, :].astype(np.float32)
-    As = (basis @ th.astype(np.float64).T).T.reshape(n_img, -1, 2, 3).astype(np.float32)
-    Bs = basis.T.reshape(basis.shape[1], -1, 2, 3).astype(np.float32)
-    lin = np.linspace(0, 1, SIZE, dtype=np.float32)
-    gx, gy = np.meshgrid(lin, lin, indexing='xy')
-    grid = np.stack([gx.reshape(-1), gy.reshape(-1)]).astype(np.float32)
-    return (th, data[:n_img].numpy(), target[:n_img].numpy(), grid, As, Bs), Tm
-
-
-def make_inputs_cpu(T):
-    d = T.get_theta_dim()
-    theta = THETA_STD * torch.randn(BATCH, d, generator=torch.Generator().manual_seed(0))
-    raw = torch.rand(BATCH, CHANNELS, SIZE, SIZE, generator=torch.Generator().manual_seed(1))
-    data = F.avg_pool2d(raw, kernel_size=5, stride=1, padding=2, count_include_pad=False)
-    # the target only enters the loss value; a smoothed copy keeps the sample self-contained
-    target = F.avg_pool2d(data, kernel_size=3, stride=1, padding=1, count_include_pad=False)
-    return theta, data.contiguous(), target.contiguous()
-
-
-def run_cpu_baseline(steps, n_img):
-    """Time the reference CPU path on n_img images; returns points/s and info."""
-    from oracle.oracle import Oracle
-    from libcpab_gb300.tessellation import make_tessellation
+def run_cpu_baseline(steps, n_img, given=None):
+    """Time the reference CPU path on n_img images (median of `steps`);
+    returns (cpu_baseline dict, sample)."""
+    from oracle.oracle import Oracle, RefLib
     orc = Oracle()
     threads = orc.num_threads()
-
-    class _T:
-        pass
-    T = _T()
-    tess = make_tessellation(NC, True, False)
-    T.params = _T()
-    T.params.basis = tess.B
-    T.get_theta_dim = lambda: tess.B.shape[1]
-    sample, Tm = cpu_sample(T, n_img)
+    try:
+        ref, kind = RefLib(), 'reference'
+    except (OSError, FileNotFoundError):
+        ref, kind = None, 'port'
+    s = cpu_sample(n_img, given)
     times = []
     for _ in range(max(1, steps)):
         t0 = time.perf_counter()
-        cpu_reference_step(sample, orc, Tm, NC)
+        cpu_reference_step(s, orc, ref, threads)
         times.append(time.perf_counter() - t0)
     pts = n_img * SIZE * SIZE
-    return pts / statistics.median(times), threads, \
-        '%d of 64 images (%d points) per step, median of %d' % (n_img, pts, len(times))
+    what = ("the reference's own libcpab/core/cpab_ops.cpp forward and analytic-gradient ops "
+            "(oracle/_ref) on %d threads over (theta, point-chunk) slices" % threads
+            if ref is not None else
+            "the C restatement of libcpab/core/cpab_ops.cpp (oracle/, OpenMP, %d threads)"
+            % threads)
+    cb = {'value': pts / statistics.median(times), 'unit': 'points/s', 'cores': threads,
+          'kind': kind, 'seconds_per_step': times,
+          'sample': '%d of 64 images (%d points) per step, median of %d steps, loss = MSE '
+                    'against the second-theta warp; %s; interpolation and its backward: the C '
+                    'restatement of libcpab/pytorch/interpolation.py' % (n_img, pts,
+                                                                         len(times), what)}
+    return cb, s
+
+
+def check_vs_fp64(s, chk):
+    """The GPU's results on the sample images of the timed step, checked:
+    trajectories against the FP64 oracle of the same scheme (C++ cell rules,
+    boundary ties classified), the warped images against the reference's
+    interpolation of the GPU's grid, dtheta and d(data) against the
+    reference's gradient algorithm (C restatement) on the GPU's grid.
+    chk: out [n, 2, nP] and cells [n, nP, 50] (traced integration), image
+    [n, C, H, W], dtheta [n, d], ddata [n, C, H, W]."""
+    from oracle.oracle import Oracle, numpy_transform_grid
+    orc = Oracle()
+    out, cells = chk['out'], chk['cells']
+    ref, cells64, marg = numpy_transform_grid(s['basis'], s['theta'], s['grid'], NC, NSTEPS,
+                                              return_cells=True, return_margin='steps',
+                                              semantics='cpp')
+    diff = cells != cells64
+    tie = diff.any(axis=2)
+    err = np.abs(out - ref).max(axis=1)
+    first = diff.argmax(axis=2)
+    ti, pi = np.nonzero(tie)
+    fm = marg[ti, pi, first[ti, pi]] if ti.size else np.zeros(0)
+    clean = err[~tie]
+    img = orc.interpolate(s['data'], out, [SIZE, SIZE])
+    gout = (2.0 * (img - s['target']) / s['n_total']).astype(np.float32)
+    dd_ref, dgrid = orc.interpolate_backward(s['data'], out, [SIZE, SIZE], gout)
+    dth_ref = orc.backward(NC, NSTEPS, s['grid'], s['A'], s['B'], dgrid)
+    rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+    r = {'sample': '%d of 64 images: %d trajectories of the timed inputs' % (out.shape[0],
+                                                                            err.size),
+         'clean_max_err': float(clean.max()) if clean.size else 0.0,
+         'clean_p99_err': float(np.quantile(clean, 0.99)) if clean.size else 0.0,
+         'tie_trajectories': int(tie.sum()),
+         'tie_first_margin_max': float(fm.max()) if fm.size else 0.0,
+         'image_max_abs_diff_vs_reference_interpolation': float(np.abs(chk['image'] - img).max()),
+         'dtheta_rel_err_vs_reference_gradient': rel(chk['dtheta'], dth_ref),
+         'ddata_rel_err_vs_reference': rel(chk['ddata'], dd_ref),
+         'gates': 'point error <= 1e-5 on trajectories with the FP64 oracle\'s cells, every '
+                  'other trajectory first diverging within 1e-6 of a decision boundary; '
+                  'dtheta <= 1e-4 and d(data) <= 1e-5 relative to the reference algorithm '
+                  'on the same warped grid'}
+    r['pass'] = bool(r['clean_max_err'] <= 1e-5 and r['tie_first_margin_max'] < 1e-6 and
+                     r['dtheta_rel_err_vs_reference_gradient'] <= 1e-4 and
+                     r['ddata_rel_err_vs_reference'] <= 1e-5)
+    return r
 
 
 def run_cpu_numpy(n_img=1):
@@ -864,17 +1060,21 @@ def main():
     if args.impl == 'reference':
         if rank != 0:
             return
-        v, cores, sample = run_cpu_baseline(max(1, args.steps // 4), args.cpu_sample_images)
+        # a bounded sample per step (the reference's CPU path is ~1e4x slower
+        # than the GPU): median of a few steps after one warm-up step
+        steps = max(CPU_STEPS, min(args.steps, 5))
+        run_cpu_baseline(1, args.cpu_sample_images)
+        cb, _ = run_cpu_baseline(steps, args.cpu_sample_images)
+        v = cb['value']
         line = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'points/s',
                 'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
                 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
                 'dtype': 'f32', 'data': 'synthetic',
                 'config': {**workload_config(BATCH), 'parallelism': 'cpu',
-                           'step': "the reference's CPU implementation (its C++ op and "
-                                   "interpolation, restated in oracle/) on a sample of the "
-                                   "batch, see cpu_baseline.sample"},
-                'cpu_baseline': {'value': v, 'unit': 'points/s', 'cores': cores,
-                                 'kind': 'port', 'sample': sample},
+                           'step': "the reference's CPU implementation on a sample of the "
+                                   "batch (%d steps timed, median), see cpu_baseline.sample"
+                                   % steps},
+                'cpu_baseline': cb,
                 'e2e': {'value': v, 'unit': 'points/s', 'h2d_bytes_per_step': 0,
                         'd2h_bytes_per_step': 0}}
         print(json.dumps(line))
@@ -890,15 +1090,18 @@ def main():
               'aligner': lambda: run_aligner(device),
               'exact': lambda: run_exact_flow(device, args.steps, flush),
               'points': lambda: run_ragged_points(device, args.steps, flush),
-              'mixed': lambda: run_mixed_images(device, args.steps, flush)}[args.leg]
+              'mixed': lambda: run_mixed_images(device, args.steps, flush),
+              'plain': lambda: run_plain_leg(device, args.steps, flush)}[args.leg]
         print(json.dumps({'leg': args.leg, 'result': fn()}))
         return
     res = run_gb300(args)
     if rank == 0 and res is not None:
+        check = res.pop('_check', None)
         if world == 1 and not args.no_cpu_baseline:
-            v, cores, sample = run_cpu_baseline(1, args.cpu_sample_images)
-            res['cpu_baseline'] = {'value': v, 'unit': 'points/s', 'cores': cores,
-                                   'kind': 'port', 'sample': sample}
+            cb, sample = run_cpu_baseline(CPU_STEPS, args.cpu_sample_images,
+                                          given=check['inputs'])
+            res['cpu_baseline'] = cb
+            res['error_vs_fp64'] = check_vs_fp64(sample, check)
             res['cpu_numpy_forward'] = run_cpu_numpy()
         print(json.dumps(res))
 

@@ -3,9 +3,11 @@
 * oracle/libcpab_oracle.so -- the C restatement in oracle/cpab_oracle.c,
   built wherever gcc exists (here and on the GPU host).
 * oracle/_ref/libcpab_ref.so -- the reference's own CPU ops
-  (libcpab/core/cpab_ops.cpp) compiled from the read-only reference checkout
-  with oracle/ref_shim.cpp.  Built only when that checkout is present; the
-  output stays out of version control.
+  (libcpab/core/cpab_ops.cpp) compiled with oracle/ref_shim.cpp from the
+  read-only reference checkout or, where the checkout is absent (a machine
+  the working tree was copied to), from the unmodified copy of the reference
+  package in baseline/_ref/libcpab (baseline/plain_gpu.py makes it).  Built
+  only when one of the two exists; the output stays out of version control.
 
 Both are built without FMA contraction so x86-64 and aarch64 round alike.
 """
@@ -16,6 +18,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 REFERENCE_ROOT = os.environ.get('CPAB_REFERENCE_ROOT', '/root/reference')
 REF_CORE = os.path.join(REFERENCE_ROOT, 'libcpab', 'core')
+REF_CORE_COPY = os.path.join(os.path.dirname(HERE), 'baseline', '_ref', 'libcpab', 'core')
 ORACLE_SO = os.path.join(HERE, 'libcpab_oracle.so')
 REF_SO = os.path.join(HERE, '_ref', 'libcpab_ref.so')
 
@@ -40,14 +43,15 @@ def build_oracle(force=False):
 
 def build_ref(force=False):
     """Compile the reference's CPU ops; returns the .so path or None."""
-    cpp = os.path.join(REF_CORE, 'cpab_ops.cpp')
+    core = REF_CORE if os.path.exists(os.path.join(REF_CORE, 'cpab_ops.cpp')) else REF_CORE_COPY
+    cpp = os.path.join(core, 'cpab_ops.cpp')
     shim = os.path.join(HERE, 'ref_shim.cpp')
     if not os.path.exists(cpp):
         return REF_SO if os.path.exists(REF_SO) else None
     if force or _stale(REF_SO, [cpp, shim]):
         os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
         tmp = REF_SO + '.tmp%d' % os.getpid()
-        subprocess.check_call(['g++', *_FLAGS, '-I', REF_CORE, shim, cpp, '-o', tmp])
+        subprocess.check_call(['g++', *_FLAGS, '-I', core, shim, cpp, '-o', tmp])
         os.replace(tmp, REF_SO)
     return REF_SO
 

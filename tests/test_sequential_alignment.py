@@ -12,6 +12,11 @@
   gradient.
 * alignment_by_gradient replayed as a CUDA graph follows the eager loop, and
   both reduce the loss.
+* Against the oracle: each composed stage against the FP64 oracle, the final
+  sampling against the oracle's interpolation, the last theta's gradient
+  against the reference's algorithm (test_sequential_vs_oracle); three Adam
+  iterations of alignment_by_gradient against an FP64 restatement of the
+  reference's loop (test_aligner_gradient_vs_oracle).
 """
 import pytest
 import torch
@@ -127,3 +132,138 @@ def test_aligner_sampling(cuda):
     T, x1, x2 = _pair(cuda)
     th = CpabAligner(T).alignment_by_sampling(x1, x2, maxiter=10)
     assert th.shape == (1, T.get_theta_dim()) and torch.isfinite(th).all()
+
+
+@pytest.mark.parametrize('ncs,shape,outsize', [
+    ([[2, 2], [3, 3], [2, 3]], (3, 2, 40, 30), (36, 28)),
+    ([[10], [20]], (3, 2, 100), (80,)),
+    ([[2, 2, 2], [3, 3, 3]], (3, 1, 12, 10, 14), (12, 10, 14)),
+])
+def test_sequential_vs_oracle(ncs, shape, outsize, cuda, oracle):
+    """Composition against the oracle (libcpab/sequential.py:91-128): every
+    stage's map against the FP64 oracle of the same scheme applied to the
+    GPU's grid before that stage (<= 1e-5 of the domain width on trajectories
+    with the oracle's cells; other trajectories are boundary ties), the final
+    sampling bit-identical to the oracle's interpolation of the final grid,
+    and the gradient of the last theta (the only one the reference's
+    semantics train) within 1e-4 of the reference's algorithm, d(data) within
+    1e-5."""
+    import numpy as np
+    from libcpab_gb300 import CpabSequential, _native as N
+    from libcpab_gb300.functions import basis_on
+    from oracle.oracle import numpy_transform_grid
+    Ts, thetas = _stages(ncs, cuda)
+    data = _data(shape, cuda)
+    th = [t.clone().requires_grad_(True) for t in thetas]
+    dd = data.clone().requires_grad_(True)
+    out = CpabSequential(*Ts).transform_data(dd, th, outsize)
+    w = torch.randn(out.shape, generator=torch.Generator().manual_seed(9)).to(cuda)
+    (out * w).sum().backward()
+    grid = Ts[0].uniform_meshgrid(outsize)
+    grids = [grid]
+    for T, t in zip(Ts, thetas):
+        grids.append(T.transform_grid(grids[-1], t))
+    ndim = len(outsize)
+    for k, (T, t) in enumerate(zip(Ts, thetas)):
+        nc = list(ncs[k])
+        _, _, E = N.cell_tables(nc, 50, t, basis_on(T.params, cuda))
+        src = grids[k]
+        out_t, cells = N.integrate_trace(nc, 50, src, E)
+        assert torch.equal(out_t, grids[k + 1])
+        src_np = src.cpu().numpy()
+        for b in range(t.shape[0]):
+            p = src_np if src_np.ndim == 2 else src_np[b]
+            ref, c64, marg = numpy_transform_grid(T.params.basis, t[b:b + 1].cpu().numpy(), p,
+                                                  nc, 50, return_cells=True,
+                                                  return_margin='steps', semantics='cpp')
+            cg = cells[b:b + 1].cpu().numpy()
+            tie = (cg != c64).any(axis=2)
+            err = np.abs(out_t[b:b + 1].cpu().numpy() - ref).max(axis=1)
+            assert (err[~tie] <= 1e-5).all(), float(err[~tie].max())
+            first = (cg != c64).argmax(axis=2)
+            ti, pi = np.nonzero(tie)
+            assert (marg[ti, pi, first[ti, pi]] < 1e-6).all()
+    final = grids[-1].cpu().numpy()
+    img_o = oracle.interpolate(data.cpu().numpy(), final, outsize)
+    assert np.array_equal(out.detach().cpu().numpy(), img_o)
+    ddata_o, dgrid_o = oracle.interpolate_backward(data.cpu().numpy(), final, outsize,
+                                                   w.cpu().numpy())
+    rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+    assert rel(dd.grad.cpu().numpy(), ddata_o) <= 1e-5
+    T = Ts[-1]
+    B = T.params.basis
+    A, _, _ = N.cell_tables(list(ncs[-1]), 50, thetas[-1], basis_on(T.params, cuda),
+                            want_E=False)
+    Bs = B.T.reshape(B.shape[1], -1, ndim, ndim + 1).astype(np.float32)
+    dth_o = oracle.backward(list(ncs[-1]), 50, grids[-2].cpu().numpy(), A.cpu().numpy(), Bs,
+                            dgrid_o)
+    assert rel(th[-1].grad.cpu().numpy(), dth_o) <= 1e-4
+    for t in th[:-1]:
+        assert torch.count_nonzero(t.grad) == 0
+
+
+def test_aligner_gradient_vs_oracle(cuda, oracle):
+    """alignment_by_gradient against the reference's loop (libcpab/alignment.py:
+    60-87), iteration by iteration on the GPU's own theta path (theta_k from
+    runs of k iterations; each starts at identity(1, 1e-6) and is
+    deterministic).  At theta_{k-1}: the loss ||transform_data(x1, theta) - x2||
+    against the FP64 oracle's warp and the oracle's interpolation (1e-5
+    relative), the gradient the loop uses against the reference's algorithm
+    (interpolation adjoint, then its analytic gradient, on the GPU's warped
+    grid and A table; 1e-4 relative); and
+    theta_k against torch's Adam update (betas 0.9 / 0.999, eps 1e-8)
+    restated in float64 on the GPU's gradients (1e-5 relative).  Adam's first
+    steps are nearly lr * sign(g), so two independent runs would amplify the
+    sign of near-zero gradient components; comparing on one theta path
+    checks the loss, the gradient and the update each on their own."""
+    import numpy as np
+    from libcpab_gb300 import CpabAligner, _native as N
+    from libcpab_gb300.functions import basis_on
+    from oracle.oracle import numpy_transform_grid
+    T, x1, x2 = _pair(cuda)
+    iters, lr = 3, 1e-2
+    path = [T.identity(1, epsilon=1e-6).detach()]
+    for k in range(1, iters + 1):
+        path.append(CpabAligner(T).alignment_by_gradient(x1, x2, maxiter=k, lr=lr).detach())
+    A = CpabAligner(T)
+    A.alignment_by_gradient(x1, x2, maxiter=iters, lr=lr)
+    losses_gpu = A.losses.cpu().numpy()
+    B = T.params.basis
+    d = B.shape[1]
+    x1n, x2n = x1.cpu().numpy(), x2.cpu().numpy()
+    grid = T.uniform_meshgrid((48, 48)).cpu().numpy()
+    Bs = B.T.reshape(d, -1, 2, 3).astype(np.float32)
+    rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+    m = np.zeros(d)
+    v = np.zeros(d)
+    b1, b2, eps = 0.9, 0.999, 1e-8
+    for k in range(1, iters + 1):
+        th = path[k - 1]
+        t = th.clone().requires_grad_(True)
+        torch.norm(T.transform_data(x1, t, outsize=x1.shape[2:]) - x2).backward()
+        g_gpu = t.grad.double().cpu().numpy()[0]
+        th32 = th.cpu().numpy()
+        gt = numpy_transform_grid(B, th32, grid, [3, 3], 50, semantics='cpp').astype(np.float32)
+        out = oracle.interpolate(x1n, gt, (48, 48))
+        r = out.astype(np.float64) - x2n
+        loss = float(np.sqrt((r ** 2).sum()))
+        assert abs(losses_gpu[k - 1] - loss) <= 1e-5 * loss, (k, losses_gpu[k - 1], loss)
+        # the gradient on the GPU's own warped grid: near the identity every
+        # meshgrid point sits on a pixel knot, where the bilinear gradient
+        # jumps, so which side a point falls on is decided by its last bits
+        gg = T.transform_grid(T.uniform_meshgrid((48, 48)), th).cpu().numpy()
+        og = oracle.interpolate(x1n, gg, (48, 48)).astype(np.float64) - x2n
+        lg = float(np.sqrt((og ** 2).sum()))
+        _, dgrid = oracle.interpolate_backward(x1n, gg, (48, 48), (og / lg).astype(np.float32))
+        # the GPU's own A table: near the identity many meshgrid points sit on
+        # cell faces at every step, where the reference-mode gradient (which
+        # depends on the chosen cell) is decided by the last bits of A
+        As, _, _ = N.cell_tables([3, 3], 50, th, basis_on(T.params, cuda), want_E=False)
+        g_o = oracle.backward([3, 3], 50, grid, As.cpu().numpy(), Bs, dgrid)[0]
+        assert rel(g_gpu, g_o) <= 1e-4, (k, rel(g_gpu, g_o))
+        m = b1 * m + (1 - b1) * g_gpu
+        v = b2 * v + (1 - b2) * g_gpu * g_gpu
+        denom = np.sqrt(v) / np.sqrt(1 - b2 ** k) + eps
+        want = th32.astype(np.float64)[0] - (lr / (1 - b1 ** k)) * (m / denom)
+        got = path[k].cpu().numpy()[0]
+        assert rel(got, want) <= 1e-5, (k, rel(got, want))
