@@ -455,6 +455,78 @@ CPAB_API int cpab_interpolate_ragged_backward(int ndim, int S, int C, const long
                                               float *ddata, float *dgrid, void *stream);
 
 /*
+ * Autotuner.  Each *_tune call takes the arguments of the call it tunes
+ * (cpab_integrate, cpab_backward, cpab_transform_data,
+ * cpab_transform_data_backward, cpab_ragged_points_forward / _backward),
+ * times that kernel's launch shapes on them -- one warm-up launch, then the
+ * best of three timed with CUDA events on the stream -- and keeps the fastest
+ * for every later call on the same problem: the same device, tessellation,
+ * nsteps, gradient mode (backward kernels other than cpab_backward, whose
+ * shape serves all modes) and sizes (points and theta count; image count,
+ * output size and C; set count and total points).  It then runs the chosen
+ * shape once more, leaving the outputs of a plain call.  Candidates:
+ *   forward kernels: 64 / 128 / 256 threads per CTA x 1 / 2 points per
+ *     thread (1 / 2 / 4 for the ragged point sets);
+ *   adjoint kernels: 64 / 128 / 256 threads x per-warp tables in shared or
+ *     (2D, 3D) global memory x the planner's CTA count per theta or image,
+ *     half of it and twice it (the ragged point-set adjoint: threads only).
+ * force (may be NULL) names one shape to keep instead of timing: it is
+ * validated, stored and run (a way to restore shapes saved from an earlier
+ * tuning run).  shape (may be NULL) receives the kept shape as
+ * CPAB_SHAPE_FIELDS ints {threads per CTA, points per thread (0: not used),
+ * CTAs per theta or image (0: not used), table staging (0 shared, 1 global,
+ * -1: not used)}; best_ms (may be NULL) its time (0 when forced).
+ *
+ * A shape only redistributes work over threads and CTAs: every point follows
+ * the same arithmetic, so point outputs (out, dpoints) are identical for all
+ * shapes and sums over points (dtheta, d(data)) differ only in the order of
+ * their float additions.  The backward tuners allocate their own workspace;
+ * after tuning, the *_workspace queries return the size for the kept shape.
+ * Tuning synchronises the stream and refuses to run while it is captured.
+ */
+#define CPAB_SHAPE_FIELDS 4
+
+CPAB_API int cpab_integrate_tune(int ndim, const int *nc, int nsteps, const float *points,
+                                 int broadcast, long long nP, const float *E, int n_theta,
+                                 float *out, const int *force, int *shape, float *best_ms,
+                                 void *stream);
+
+CPAB_API int cpab_backward_tune(int ndim, const int *nc, int nsteps, int mode,
+                                const float *points, int broadcast, long long nP, const float *A,
+                                const float *E, int n_theta, const float *basis, int d,
+                                const float *grad_out, float *dtheta, float *dpoints,
+                                const int *force, int *shape, float *best_ms, void *stream);
+
+CPAB_API int cpab_transform_data_tune(int ndim, const int *nc, int nsteps, const float *lin,
+                                      const int *outsize, const float *E, int nb,
+                                      const float *data, int C, const int *size, float *out,
+                                      float *grid_out, const int *force, int *shape,
+                                      float *best_ms, void *stream);
+
+CPAB_API int cpab_transform_data_backward_tune(int ndim, const int *nc, int nsteps, int mode,
+                                               const float *lin, const int *outsize,
+                                               const float *A, const float *E,
+                                               const float *grid_saved, int nb,
+                                               const float *data, int C, const int *size,
+                                               const float *basis, int d, const float *grad_out,
+                                               float *ddata, float *dtheta, const int *force,
+                                               int *shape, float *best_ms, void *stream);
+
+/* kind 0: cpab_ragged_points_forward (E, points -> out); kind 1:
+ * cpab_ragged_points_backward (A, E, points, grad_out -> dtheta, dpoints). */
+CPAB_API int cpab_ragged_points_tune(int kind, int ndim, const int *nc, int nsteps, int mode,
+                                     const float *A, const float *E, int S,
+                                     const long long *offsets, long long total,
+                                     const float *basis, int d, const float *points,
+                                     const float *grad_out, float *out, float *dtheta,
+                                     float *dpoints, const int *force, int *shape,
+                                     float *best_ms, void *stream);
+
+/* Forget every kept launch shape (all kinds, all devices) except those of
+ * cpab_ragged1d_tune; later calls use the built-in heuristics again. */
+CPAB_API void cpab_tune_reset(void);
+
+/*
  * Synchronise the current device and report the device error word (the
  * CPAB_DEV_* bits raised by kernels since the last clear).  clear != 0 resets
  * it.  Returns CPAB_OK, or CPAB_ERR_CUDA if the device reported an error.

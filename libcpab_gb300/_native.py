@@ -24,6 +24,7 @@ _vp = ctypes.c_void_p
 _i = ctypes.c_int
 _ll = ctypes.c_longlong
 _sz = ctypes.c_size_t
+_fp = ctypes.POINTER(ctypes.c_float)
 
 _SIGS = {
     'cpab_last_error': ([], ctypes.c_char_p),
@@ -75,6 +76,18 @@ _SIGS = {
     'cpab_interpolate_ragged': ([_i, _i, _i, _vp, _ll, _ll, _ll, _vp, _vp, _vp, _vp], _i),
     'cpab_interpolate_ragged_backward': ([_i, _i, _i, _vp, _ll, _ll, _ll, _vp, _vp, _vp, _vp, _vp,
                                           _vp], _i),
+    'cpab_integrate_tune': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _c_int_p, _c_int_p,
+                             _fp, _vp], _i),
+    'cpab_backward_tune': ([_i, _c_int_p, _i, _i, _vp, _i, _ll, _vp, _vp, _i, _vp, _i, _vp, _vp,
+                            _vp, _c_int_p, _c_int_p, _fp, _vp], _i),
+    'cpab_transform_data_tune': ([_i, _c_int_p, _i, _vp, _c_int_p, _vp, _i, _vp, _i, _c_int_p,
+                                  _vp, _vp, _c_int_p, _c_int_p, _fp, _vp], _i),
+    'cpab_transform_data_backward_tune': ([_i, _c_int_p, _i, _i, _vp, _c_int_p, _vp, _vp, _vp,
+                                           _i, _vp, _i, _c_int_p, _vp, _i, _vp, _vp, _vp,
+                                           _c_int_p, _c_int_p, _fp, _vp], _i),
+    'cpab_ragged_points_tune': ([_i, _i, _c_int_p, _i, _i, _vp, _vp, _i, _vp, _ll, _vp, _i, _vp,
+                                 _vp, _vp, _vp, _vp, _c_int_p, _c_int_p, _fp, _vp], _i),
+    'cpab_tune_reset': ([], None),
 }
 
 EXPORTED = tuple(_SIGS)
@@ -684,3 +697,147 @@ def interpolate_ragged_backward(ndim, plan, totals, data, grid, C, grad_out, wan
         int(ndim), plan.shape[0] - 1, int(C), _ptr(plan), data_points, total, tiles, _ptr(data),
         _ptr(grid), _ptr(grad_out), _ptr(ddata), _ptr(dgrid), _stream(data.device)))
     return ddata, dgrid
+
+
+# -------------------------------- autotuner --------------------------------- #
+SHAPE_FIELDS = 4   # (threads per CTA, points per thread, CTAs per theta/image, table staging)
+
+
+def _shape_io(force):
+    """(force array or None, shape array, best-ms float) for a *_tune call."""
+    f = None
+    if force is not None:
+        force = tuple(int(v) for v in force)
+        if len(force) != SHAPE_FIELDS:
+            raise ValueError('a launch shape has %d fields' % SHAPE_FIELDS)
+        f = (ctypes.c_int * SHAPE_FIELDS)(*force)
+    return f, (ctypes.c_int * SHAPE_FIELDS)(), ctypes.c_float(0.0)
+
+
+def integrate_tune(nc, nsteps, points, E, force=None):
+    """Autotune (or, with force, pin) the launch shape of integrate() on these
+    inputs.  Returns (shape tuple, best ms, out)."""
+    _require(points, 'points')
+    _require(E, 'E')
+    ndim = len(nc)
+    n_theta = E.shape[0]
+    broadcast = int(points.dim() == 3 and points.shape[0] == n_theta)
+    nP = points.shape[-1]
+    out = torch.empty((n_theta, ndim, nP), device=points.device, dtype=torch.float32)
+    f, sh, ms = _shape_io(force)
+    _check(load().cpab_integrate_tune(ndim, _ints(nc), int(nsteps), _ptr(points), broadcast, nP,
+                                      _ptr(E), n_theta, _ptr(out), f, sh, ctypes.byref(ms),
+                                      _stream(points.device)))
+    return tuple(sh), ms.value, out
+
+
+def backward_tune(nc, nsteps, mode, points, A, E, basis, grad_out, want_dpoints=False,
+                  force=None):
+    """Autotune (or pin) the launch shape of backward().  Returns (shape tuple,
+    best ms, dtheta, dpoints or None)."""
+    _require(points, 'points')
+    _require(A, 'A')
+    _require(basis, 'basis')
+    _require(grad_out, 'grad_out')
+    if mode == GRAD_EXACT:
+        _require(E, 'E')
+    ndim = len(nc)
+    n_theta = A.shape[0]
+    d = basis.shape[1]
+    broadcast = int(points.dim() == 3 and points.shape[0] == n_theta)
+    nP = points.shape[-1]
+    dev = points.device
+    dtheta = torch.empty((n_theta, d), device=dev, dtype=torch.float32)
+    dpoints = torch.empty((n_theta, ndim, nP), device=dev, dtype=torch.float32) \
+        if want_dpoints else None
+    f, sh, ms = _shape_io(force)
+    _check(load().cpab_backward_tune(ndim, _ints(nc), int(nsteps), int(mode), _ptr(points),
+                                     broadcast, nP, _ptr(A), _ptr(E), n_theta, _ptr(basis), d,
+                                     _ptr(grad_out), _ptr(dtheta), _ptr(dpoints), f, sh,
+                                     ctypes.byref(ms), _stream(dev)))
+    return tuple(sh), ms.value, dtheta, dpoints
+
+
+def transform_data_tune(nc, nsteps, lin, outsize, E, data, save_grid=False, force=None):
+    """Autotune (or pin) the fused forward's launch shape.  Returns (shape
+    tuple, best ms, out, grid or None)."""
+    _require(lin, 'lin')
+    _require(E, 'E')
+    _require(data, 'data')
+    ndim = len(nc)
+    nb, C = data.shape[0], data.shape[1]
+    nP = 1
+    for o in outsize:
+        nP *= int(o)
+    out = torch.empty((nb, C, *[int(o) for o in outsize]), device=data.device,
+                      dtype=torch.float32)
+    grid = torch.empty((nb, ndim, nP), device=data.device, dtype=torch.float32) \
+        if save_grid else None
+    f, sh, ms = _shape_io(force)
+    _check(load().cpab_transform_data_tune(ndim, _ints(nc), int(nsteps), _ptr(lin),
+                                           _ints(outsize), _ptr(E), nb, _ptr(data), C,
+                                           _ints(data.shape[2:]), _ptr(out), _ptr(grid), f, sh,
+                                           ctypes.byref(ms), _stream(data.device)))
+    return tuple(sh), ms.value, out, grid
+
+
+def transform_data_backward_tune(nc, nsteps, mode, lin, outsize, A, E, grid_saved, data, basis,
+                                 grad_out, want_ddata=True, force=None):
+    """Autotune (or pin) the fused backward's launch shape.  Returns (shape
+    tuple, best ms, ddata or None, dtheta)."""
+    _require(lin, 'lin')
+    _require(A, 'A')
+    _require(data, 'data')
+    _require(basis, 'basis')
+    _require(grad_out, 'grad_out')
+    if mode == GRAD_EXACT:
+        _require(E, 'E')
+    else:
+        _require(grid_saved, 'grid_saved')
+    ndim = len(nc)
+    nb, C = data.shape[0], data.shape[1]
+    d = basis.shape[1]
+    dev = data.device
+    dtheta = torch.empty((nb, d), device=dev, dtype=torch.float32)
+    ddata = torch.empty_like(data) if want_ddata else None
+    f, sh, ms = _shape_io(force)
+    _check(load().cpab_transform_data_backward_tune(
+        ndim, _ints(nc), int(nsteps), int(mode), _ptr(lin), _ints(outsize), _ptr(A), _ptr(E),
+        _ptr(grid_saved), nb, _ptr(data), C, _ints(data.shape[2:]), _ptr(basis), d,
+        _ptr(grad_out), _ptr(ddata), _ptr(dtheta), f, sh, ctypes.byref(ms), _stream(dev)))
+    return tuple(sh), ms.value, ddata, dtheta
+
+
+def ragged_points_tune(kind, nc, nsteps, mode, A, E, offsets, points, basis=None, grad_out=None,
+                       want_dpoints=False, force=None):
+    """Autotune (or pin) the ragged point-set forward (kind 0) or backward
+    (kind 1) launch shape.  Returns (shape tuple, best ms, out or None,
+    dtheta or None, dpoints or None)."""
+    ndim, S, total = _points_common(nc, offsets, points)
+    dev = points.device
+    out = dtheta = dpoints = None
+    d = 0
+    if kind == 0:
+        _require(E, 'E')
+        out = torch.empty_like(points)
+    else:
+        _require(A, 'A')
+        _require(basis, 'basis')
+        _require(grad_out, 'grad_out')
+        if E is not None:
+            _require(E, 'E')
+        d = basis.shape[1]
+        dtheta = torch.empty((S, d), device=dev, dtype=torch.float32)
+        dpoints = torch.empty_like(points) if want_dpoints else None
+    f, sh, ms = _shape_io(force)
+    _check(load().cpab_ragged_points_tune(int(kind), ndim, _ints(nc), int(nsteps), int(mode),
+                                          _ptr(A), _ptr(E), S, _ptr(offsets), total,
+                                          _ptr(basis), d, _ptr(points), _ptr(grad_out),
+                                          _ptr(out), _ptr(dtheta), _ptr(dpoints), f, sh,
+                                          ctypes.byref(ms), _stream(dev)))
+    return tuple(sh), ms.value, out, dtheta, dpoints
+
+
+def tune_reset():
+    """Forget every kept launch shape (the ragged 1D series' excepted)."""
+    load().cpab_tune_reset()

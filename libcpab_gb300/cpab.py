@@ -273,6 +273,32 @@ class Cpab(object):
         self._check_type(theta); self._check_device(theta)
         return self.backend.ragged_mse(values, target, offsets, theta, self.params, **kwargs)
 
+    # ------------------------------------------------------------- tuning --
+    def tune_transform_grid(self, grid, theta, backward=True, force=None):
+        """Autotune the launch shapes of transform_grid (and its backward) for
+        these shapes (extension); later calls on the same problem use them.
+        Returns {'forward': (shape, ms), 'backward': (shape, ms)}."""
+        self._check_type(grid); self._check_device(grid)
+        self._check_type(theta); self._check_device(theta)
+        from .tuning import tune_transform_grid
+        return tune_transform_grid(grid, theta, self.params, backward=backward, force=force)
+
+    def tune_transform_data(self, data, theta, outsize, backward=True, force=None):
+        """Autotune the fused transform_data kernels for these shapes (extension)."""
+        self._check_type(data); self._check_device(data)
+        self._check_type(theta); self._check_device(theta)
+        from .tuning import tune_transform_data
+        return tune_transform_data(data, theta, self.params, outsize, backward=backward,
+                                   force=force)
+
+    def tune_transform_grid_ragged(self, points, offsets, theta, backward=True, force=None):
+        """Autotune the ragged point-set kernels for these sets (extension)."""
+        self._check_type(points); self._check_device(points)
+        self._check_type(theta); self._check_device(theta)
+        from .tuning import tune_transform_grid_ragged
+        return tune_transform_grid_ragged(points, offsets, theta, self.params,
+                                          backward=backward, force=force)
+
     def calc_vectorfield(self, grid, theta):
         self._check_type(grid); self._check_device(grid)
         self._check_type(theta); self._check_device(theta)

@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256)
 // ------------------------------ planning -------------------------------------
 template <int N, int MODE, typename CT>
 static bool plan_t(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan,
-                   bool allow_global) {
+                   bool allow_global, const LaunchShape &sh) {
     int block = 0, per_sm = 0;
     bool global_gw = false;
     size_t smem = 0;
@@ -106,11 +106,11 @@ static bool plan_t(const Tess &t, int nsteps, long long nP, int n_theta, Adjoint
     if constexpr (N >= 2)
         if (allow_global) kg = k_adjoint<N, MODE, CT, true>;
     if (!adjoint_shape<N, CT>(k_adjoint<N, MODE, CT, false>, kg, t.nC, nsteps, &block,
-                              &global_gw, &smem, &per_sm))
+                              &global_gw, &smem, &per_sm, sh.block, sh.staging))
         return false;
     const long long tiles = (nP + block - 1) / block;
     const long long target = 2ll * num_sms() * per_sm;
-    long long parts = (target + n_theta - 1) / n_theta;
+    long long parts = sh.parts > 0 ? sh.parts : (target + n_theta - 1) / n_theta;
     if (parts > tiles) parts = tiles;
     if (parts < 1) parts = 1;
     plan->block = block;
@@ -124,14 +124,15 @@ static bool plan_t(const Tess &t, int nsteps, long long nP, int n_theta, Adjoint
 }
 
 static bool plan_adjoint_mode_uncached(const Tess &t, int nsteps, int mode, long long nP,
-                                       int n_theta, AdjointPlan *plan, bool allow_global) {
+                                       int n_theta, AdjointPlan *plan, bool allow_global,
+                                       const LaunchShape &sh) {
     const bool small = t.nC <= 256;
-#define CPAB_PLAN(N)                                                                          \
-    if (mode != 1)                                                                            \
-        return small ? plan_t<N, 0, uint8_t>(t, nsteps, nP, n_theta, plan, allow_global)      \
-                     : plan_t<N, 0, uint16_t>(t, nsteps, nP, n_theta, plan, allow_global);    \
-    return small ? plan_t<N, 1, uint8_t>(t, nsteps, nP, n_theta, plan, allow_global)          \
-                 : plan_t<N, 1, uint16_t>(t, nsteps, nP, n_theta, plan, allow_global);
+#define CPAB_PLAN(N)                                                                               \
+    if (mode != 1)                                                                                 \
+        return small ? plan_t<N, 0, uint8_t>(t, nsteps, nP, n_theta, plan, allow_global, sh)       \
+                     : plan_t<N, 0, uint16_t>(t, nsteps, nP, n_theta, plan, allow_global, sh);     \
+    return small ? plan_t<N, 1, uint8_t>(t, nsteps, nP, n_theta, plan, allow_global, sh)           \
+                 : plan_t<N, 1, uint16_t>(t, nsteps, nP, n_theta, plan, allow_global, sh);
     switch (t.ndim) {
         case 1: { CPAB_PLAN(1) }
         case 2: { CPAB_PLAN(2) }
@@ -140,21 +141,29 @@ static bool plan_adjoint_mode_uncached(const Tess &t, int nsteps, int mode, long
 #undef CPAB_PLAN
 }
 
+// The tuned shape (cpab_backward_tune) applies to plans that may stage the
+// per-warp tables in global memory; the no-allocation entry point plans with
+// shared-memory tables only and keeps the heuristic shape.
 bool plan_adjoint_mode(const Tess &t, int nsteps, int mode, long long nP, int n_theta,
-                       AdjointPlan *plan, bool allow_global) {
+                       AdjointPlan *plan, bool allow_global, const LaunchShape *force) {
+    if (force) return plan_adjoint_mode_uncached(t, nsteps, mode, nP, n_theta, plan,
+                                                 allow_global, *force);
+    LaunchShape sh;
+    const bool tuned = allow_global &&
+                       tuned_get(kTuneAdjoint, tune_key(t, nsteps, 0, nP, n_theta, 0), &sh);
+    const int flag = (allow_global ? 1 : 0) +
+                     (tuned ? 2 * (1 + (sh.staging + 1) + 4 * (sh.block / 32) + 64 * sh.parts) : 0);
     static PlanCache cache;
-    return cache.get(0, t, nsteps, mode, nP, n_theta, allow_global ? 1 : 0, plan,
-                     [&](AdjointPlan *p) {
-                         return plan_adjoint_mode_uncached(t, nsteps, mode, nP, n_theta, p,
-                                                           allow_global);
-                     });
+    return cache.get(0, t, nsteps, mode, nP, n_theta, flag, plan, [&](AdjointPlan *p) {
+        return plan_adjoint_mode_uncached(t, nsteps, mode, nP, n_theta, p, allow_global, sh);
+    });
 }
 
 bool plan_adjoint(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan,
-                  bool allow_global) {
-    // Both modes share the shared-memory layout; plan with the larger register
-    // footprint (mode 0) so the plan is valid for either.
-    return plan_adjoint_mode(t, nsteps, 0, nP, n_theta, plan, allow_global);
+                  bool allow_global, const LaunchShape *force) {
+    // All modes share the shared-memory layout; plan with the larger register
+    // footprint (mode 0) so the plan is valid for any of them.
+    return plan_adjoint_mode(t, nsteps, 0, nP, n_theta, plan, allow_global, force);
 }
 
 template <int N, int MODE, typename CT>

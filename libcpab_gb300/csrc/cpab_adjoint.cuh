@@ -207,10 +207,13 @@ __host__ __device__ inline size_t adjoint_smem_bytes(int nC, int nsteps, int blo
 // Host: the launch shape of an adjoint kernel with the most resident warps per
 // SM among 256/128/64 threads per CTA and per-warp tables in shared memory
 // (kern_shared) or in global memory (kern_global, may be nullptr; see
-// carve_adjoint).  Ties keep shared memory and the larger CTA.
+// carve_adjoint).  Ties keep shared memory and the larger CTA.  force_block
+// (> 0) and force_staging (0 shared, 1 global; -1 either) restrict the
+// candidates (the autotuner's shapes).
 template <int N, typename CT, typename K>
 inline bool adjoint_shape(K kern_shared, K kern_global, int nC, int nsteps, int *block,
-                          bool *global_gw, size_t *smem, int *per_sm) {
+                          bool *global_gw, size_t *smem, int *per_sm, int force_block = 0,
+                          int force_staging = -1) {
     const bool allow_global = kern_global != nullptr;
     int dev = 0, max_optin = 0;
     cudaGetDevice(&dev);
@@ -219,8 +222,10 @@ inline bool adjoint_shape(K kern_shared, K kern_global, int nC, int nsteps, int 
     const int cands[3] = {256, 128, 64};
     int best = 0;
     for (int g = 0; g < (allow_global ? 2 : 1); ++g) {
+        if (force_staging >= 0 && g != force_staging) continue;
         for (int ci = 0; ci < 3; ++ci) {
             const int b = cands[ci];
+            if (force_block > 0 && b != force_block) continue;
             const size_t sm = adjoint_smem_bytes<N, CT>(nC, nsteps, b, g == 0) + 64;
             if (sm > (size_t)max_optin) continue;
             const K kern = g == 0 ? kern_shared : kern_global;

@@ -7,7 +7,9 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
+#include <vector>
 
 #include "../../include/cpab_gb300.h"
 #include "cpab_interp.cuh"
@@ -146,7 +148,7 @@ int cpab_cell_tables(int ndim, const int *nc, int nsteps, const float *theta, in
 static int integrate_common(int ndim, const int *nc, int nsteps, const float *points,
                             int broadcast, long long nP, const float *table, bool comp,
                             int n_theta, float *out, int *trace, unsigned long long *ties,
-                            void *stream) {
+                            void *stream, const LaunchShape *force = nullptr) {
     g_err[0] = 0;
     Tess t;
     int rc = make_tess(ndim, nc, &t);
@@ -158,7 +160,7 @@ static int integrate_common(int ndim, const int *nc, int nsteps, const float *po
     if (!points || !table || !out) return fail(CPAB_ERR_ARGUMENT, "points, table or out is NULL");
     unsigned *err = device_error_word();
     cudaError_t e = launch_integrate(t, nsteps, points, broadcast ? 1 : 0, nP, table, comp, n_theta,
-                                     out, trace, ties, err, as_stream(stream));
+                                     out, trace, ties, err, as_stream(stream), force);
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "integrate launch");
 }
 
@@ -212,11 +214,14 @@ size_t cpab_backward_workspace(int ndim, const int *nc, int nsteps, long long nP
     return plan.ws_floats() * sizeof(float);
 }
 
-int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *points,
-                  int broadcast, long long nP, const float *A, const float *E, int n_theta,
-                  const float *basis, int d, const float *grad_out, float *dtheta,
-                  float *dpoints, void *workspace, size_t workspace_bytes,
-                  unsigned long long *ties, void *stream) {
+}  // extern "C"
+
+static int backward_impl(int ndim, const int *nc, int nsteps, int mode, const float *points,
+                         int broadcast, long long nP, const float *A, const float *E,
+                         int n_theta, const float *basis, int d, const float *grad_out,
+                         float *dtheta, float *dpoints, void *workspace,
+                         size_t workspace_bytes, unsigned long long *ties, void *stream,
+                         const LaunchShape *force) {
     g_err[0] = 0;
     Tess t;
     int rc = make_tess(ndim, nc, &t);
@@ -238,7 +243,7 @@ int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *po
     }
     if (!points || !grad_out) return fail(CPAB_ERR_ARGUMENT, "points or grad_out is NULL");
     AdjointPlan plan;
-    if (!plan_adjoint(t, nsteps, nP, n_theta, &plan))
+    if (!plan_adjoint(t, nsteps, nP, n_theta, &plan, true, force))
         return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
     const size_t need = plan.ws_floats() * sizeof(float);
     if (!workspace || workspace_bytes < need)
@@ -253,6 +258,18 @@ int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *po
     if (d == 0) return CPAB_OK;
     e = launch_finalize(t, nsteps, mode, partials, plan.parts, A, basis, d, n_theta, dtheta, s);
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "finalize launch");
+}
+
+extern "C" {
+
+int cpab_backward(int ndim, const int *nc, int nsteps, int mode, const float *points,
+                  int broadcast, long long nP, const float *A, const float *E, int n_theta,
+                  const float *basis, int d, const float *grad_out, float *dtheta,
+                  float *dpoints, void *workspace, size_t workspace_bytes,
+                  unsigned long long *ties, void *stream) {
+    return backward_impl(ndim, nc, nsteps, mode, points, broadcast, nP, A, E, n_theta, basis, d,
+                         grad_out, dtheta, dpoints, workspace, workspace_bytes, ties, stream,
+                         nullptr);
 }
 
 int cpab_interpolate(int ndim, const float *data, int nb, int C, const int *size,
@@ -292,10 +309,12 @@ int cpab_interpolate_backward(int ndim, const float *data, int nb, int C, const 
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "interpolate backward launch");
 }
 
-int cpab_transform_data(int ndim, const int *nc, int nsteps, const float *lin,
-                        const int *outsize, const float *E, int nb, const float *data, int C,
-                        const int *size, float *out, float *grid_out,
-                        unsigned long long *ties, void *stream) {
+}  // extern "C"
+
+static int td_forward(int ndim, const int *nc, int nsteps, const float *lin, const int *outsize,
+                      const float *E, int nb, const float *data, int C, const int *size,
+                      float *out, float *grid_out, unsigned long long *ties, void *stream,
+                      const LaunchShape *force) {
     g_err[0] = 0;
     Tess t;
     int rc = make_tess(ndim, nc, &t);
@@ -307,8 +326,19 @@ int cpab_transform_data(int ndim, const int *nc, int nsteps, const float *lin,
     if (nb == 0) return CPAB_OK;
     if (!lin || !E || !data || !out) return fail(CPAB_ERR_ARGUMENT, "lin, E, data or out is NULL");
     cudaError_t e = launch_transform_data(t, nsteps, lin, outsize, E, nb, data, C, size, out,
-                                          grid_out, ties, device_error_word(), as_stream(stream));
+                                          grid_out, ties, device_error_word(), as_stream(stream),
+                                          force);
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "transform_data launch");
+}
+
+extern "C" {
+
+int cpab_transform_data(int ndim, const int *nc, int nsteps, const float *lin,
+                        const int *outsize, const float *E, int nb, const float *data, int C,
+                        const int *size, float *out, float *grid_out,
+                        unsigned long long *ties, void *stream) {
+    return td_forward(ndim, nc, nsteps, lin, outsize, E, nb, data, C, size, out, grid_out, ties,
+                      stream, nullptr);
 }
 
 int cpab_transform_grid_image(int ndim, const int *nc, int nsteps, const float *lin,
@@ -472,7 +502,8 @@ static int td_backward(int ndim, const int *nc, int nsteps, int mode, const floa
                        const float *grid_saved, int nb, const float *data, int C,
                        const int *size, const float *basis, int d, const float *grad_out,
                        float *ddata, float *dtheta, void *workspace, size_t workspace_bytes,
-                       unsigned long long *ties, void *stream, const PreStages *pre) {
+                       unsigned long long *ties, void *stream, const PreStages *pre,
+                       const LaunchShape *force = nullptr) {
     g_err[0] = 0;
     Tess t;
     int rc = make_tess(ndim, nc, &t);
@@ -492,7 +523,7 @@ static int td_backward(int ndim, const int *nc, int nsteps, int mode, const floa
     long long nP = 1;
     for (int j = 0; j < ndim; ++j) nP *= outsize[j];
     AdjointPlan plan;
-    if (!plan_transform_data_backward(t, nsteps, mode, nP, nb, &plan))
+    if (!plan_transform_data_backward(t, nsteps, mode, nP, nb, &plan, force))
         return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
     const size_t need = plan.ws_floats() * sizeof(float);
     if (!workspace || workspace_bytes < need)
@@ -893,10 +924,10 @@ static int check_ragged_points(int ndim, const int *nc, int nsteps, int S, long 
     return CPAB_OK;
 }
 
-int cpab_ragged_points_forward(int ndim, const int *nc, int nsteps, const float *E, int S,
+static int points_forward_impl(int ndim, const int *nc, int nsteps, const float *E, int S,
                                const long long *offsets, long long total, const float *points,
                                float *out, void *workspace, size_t workspace_bytes,
-                               unsigned long long *ties, void *stream) {
+                               unsigned long long *ties, void *stream, const LaunchShape *force) {
     g_err[0] = 0;
     Tess t;
     int rc = check_ragged_points(ndim, nc, nsteps, S, total, offsets, workspace,
@@ -906,16 +937,17 @@ int cpab_ragged_points_forward(int ndim, const int *nc, int nsteps, const float 
     if (!E || !points || !out) return fail(CPAB_ERR_ARGUMENT, "E, points or out is NULL");
     cudaError_t e = launch_ragged_points_forward(t, nsteps, S, offsets, total, E, points, out,
                                                  workspace, ties, device_error_word(),
-                                                 as_stream(stream));
+                                                 as_stream(stream), force);
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "ragged points forward launch");
 }
 
-int cpab_ragged_points_backward(int ndim, const int *nc, int nsteps, int mode, const float *A,
+static int points_backward_impl(int ndim, const int *nc, int nsteps, int mode, const float *A,
                                 const float *E, int S, const long long *offsets,
                                 long long total, const float *basis, int d,
                                 const float *points, const float *grad_out, float *dtheta,
                                 float *dpoints, void *workspace, size_t workspace_bytes,
-                                unsigned long long *ties, void *stream) {
+                                unsigned long long *ties, void *stream,
+                                const LaunchShape *force) {
     g_err[0] = 0;
     Tess t;
     int rc = check_ragged_points(ndim, nc, nsteps, S, total, offsets, workspace,
@@ -936,10 +968,29 @@ int cpab_ragged_points_backward(int ndim, const int *nc, int nsteps, int mode, c
     cudaError_t e = launch_ragged_points_backward(t, nsteps, mode, S, offsets, total, A, E,
                                                   points, grad_out, dpoints, basis, d,
                                                   d > 0 ? dtheta : nullptr, workspace, ties,
-                                                  device_error_word(), s);
+                                                  device_error_word(), s, force);
     if (e == cudaErrorInvalidConfiguration)
         return fail(CPAB_ERR_UNSUPPORTED, "tessellation/nsteps too large for the adjoint kernel");
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "ragged points adjoint launch");
+}
+
+int cpab_ragged_points_forward(int ndim, const int *nc, int nsteps, const float *E, int S,
+                               const long long *offsets, long long total, const float *points,
+                               float *out, void *workspace, size_t workspace_bytes,
+                               unsigned long long *ties, void *stream) {
+    return points_forward_impl(ndim, nc, nsteps, E, S, offsets, total, points, out, workspace,
+                               workspace_bytes, ties, stream, nullptr);
+}
+
+int cpab_ragged_points_backward(int ndim, const int *nc, int nsteps, int mode, const float *A,
+                                const float *E, int S, const long long *offsets,
+                                long long total, const float *basis, int d,
+                                const float *points, const float *grad_out, float *dtheta,
+                                float *dpoints, void *workspace, size_t workspace_bytes,
+                                unsigned long long *ties, void *stream) {
+    return points_backward_impl(ndim, nc, nsteps, mode, A, E, S, offsets, total, basis, d, points,
+                                grad_out, dtheta, dpoints, workspace, workspace_bytes, ties,
+                                stream, nullptr);
 }
 
 }  // extern "C"
@@ -1060,5 +1111,392 @@ int cpab_backward_noalloc(int ndim, const int *nc, int nsteps, int mode, const f
     e = launch_finalize(t, nsteps, mode, partials, plan.parts, A, basis, d, n_theta, dtheta, s);
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "finalize launch");
 }
+
+}  // extern "C"
+
+// -------------------------------- autotuner ----------------------------------
+// Each tuner times the launch shapes of one kernel family on the caller's own
+// arguments (one warm-up launch, then the best of three timed with CUDA events
+// on the caller's stream), keeps the fastest for later calls on the same
+// problem (device, tessellation, nsteps, mode, sizes) and finishes with a run
+// of the chosen shape, so its outputs are those of a plain call.  A shape
+// changes only how work is spread over threads and CTAs: every point follows
+// the same arithmetic, so outputs per point are identical and sums over
+// points (dtheta, d(data)) change only in their float summation order.
+namespace {
+
+constexpr int kSkip = -1000;   // the candidate does not apply to this problem
+
+int refuse_capture(cudaStream_t s, const char *who) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(CPAB_ERR_CUDA, "%s: cannot query the stream's capture state", who);
+    }
+    if (cap != cudaStreamCaptureStatusNone)
+        return fail(CPAB_ERR_ARGUMENT, "%s times launches; call it outside stream capture", who);
+    return CPAB_OK;
+}
+
+// Device scratch of one tuning call (freed on return).
+struct Scratch {
+    void *p = nullptr;
+    size_t bytes = 0;
+    ~Scratch() {
+        if (p) cudaFree(p);
+    }
+    int reserve(size_t b) {
+        if (b <= bytes) return CPAB_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) return cuda_fail(e, "tuning workspace");
+        bytes = b;
+        return CPAB_OK;
+    }
+};
+
+void put_shape(const LaunchShape &sh, int *shape) {
+    if (!shape) return;
+    shape[0] = sh.block;
+    shape[1] = sh.ppt;
+    shape[2] = sh.parts;
+    shape[3] = sh.staging;
+}
+
+LaunchShape get_shape(const int *v) {
+    LaunchShape sh;
+    sh.block = v[0];
+    sh.ppt = v[1];
+    sh.parts = v[2];
+    sh.staging = v[3];
+    return sh;
+}
+
+// Forward kernels: 32..256 threads (multiple of 32), ppt in {1, 2} (or
+// {1, 2, 4} for the ragged point sets).
+int check_forward_shape(const LaunchShape &sh, int max_ppt) {
+    const bool ppt_ok = sh.ppt == 1 || sh.ppt == 2 || (max_ppt >= 4 && sh.ppt == 4);
+    if (sh.block < 32 || sh.block > 256 || sh.block % 32 || !ppt_ok)
+        return fail(CPAB_ERR_ARGUMENT, "launch shape {%d, %d}: threads must be a multiple of 32 in "
+                    "[32, 256] and points per thread 1, 2%s", sh.block, sh.ppt,
+                    max_ppt >= 4 ? " or 4" : "");
+    return CPAB_OK;
+}
+
+// Adjoint kernels: 64, 128 or 256 threads; parts >= 1; staging 0 (shared) or
+// 1 (global, 2D/3D only).
+int check_adjoint_shape(const LaunchShape &sh, int ndim) {
+    if ((sh.block != 64 && sh.block != 128 && sh.block != 256) || sh.parts < 1 ||
+        sh.staging < 0 || sh.staging > 1 || (ndim == 1 && sh.staging == 1))
+        return fail(CPAB_ERR_ARGUMENT, "launch shape {%d, parts %d, staging %d}: threads 64, 128 "
+                    "or 256, parts >= 1, staging 0 or 1 (1 only in 2D/3D)", sh.block, sh.parts,
+                    sh.staging);
+    return CPAB_OK;
+}
+
+std::vector<LaunchShape> forward_candidates(int max_ppt) {
+    std::vector<LaunchShape> c;
+    for (int b : {64, 128, 256})
+        for (int p = 1; p <= max_ppt; p *= 2) {
+            LaunchShape sh;
+            sh.block = b;
+            sh.ppt = p;
+            c.push_back(sh);
+        }
+    return c;
+}
+
+// Adjoint candidates: every (threads, staging) that the planner accepts, each
+// with the planner's CTA count per theta/image and with half and twice that.
+// plan(shape, &plan) resolves a shape with parts = 0 to the planner's.
+template <typename P>
+std::vector<LaunchShape> adjoint_candidates(int ndim, P plan, size_t *ws_max) {
+    std::vector<LaunchShape> c;
+    *ws_max = 0;
+    for (int g = 0; g < (ndim >= 2 ? 2 : 1); ++g)
+        for (int b : {64, 128, 256}) {
+            LaunchShape sh;
+            sh.block = b;
+            sh.staging = g;
+            AdjointPlan pl;
+            if (!plan(sh, &pl) || pl.block != b || (pl.gw_floats != 0) != (g == 1)) continue;
+            const int base = pl.parts;
+            for (int m = 0; m < 3; ++m) {
+                const int parts = m == 0 ? base : m == 1 ? (base + 1) / 2 : base * 2;
+                if (m > 0 && (parts == base || parts > pl.tiles)) continue;
+                LaunchShape v = sh;
+                v.parts = parts;
+                AdjointPlan pv;
+                if (!plan(v, &pv)) continue;
+                v.parts = pv.parts;
+                bool dup = false;
+                for (const LaunchShape &o : c)
+                    dup |= o.block == v.block && o.staging == v.staging && o.parts == v.parts;
+                if (dup) continue;
+                c.push_back(v);
+                *ws_max = std::max(*ws_max, pv.ws_floats() * sizeof(float));
+            }
+        }
+    return c;
+}
+
+// Times run(shape) over the candidates; *best and *best_ms receive the
+// fastest.  run returns CPAB_OK, kSkip or an error code (which ends tuning).
+template <typename F>
+int time_candidates(const std::vector<LaunchShape> &cands, cudaStream_t s, F run,
+                    LaunchShape *best, float *best_ms) {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        cudaError_t e = cudaGetLastError();
+        if (e0) cudaEventDestroy(e0);
+        return cuda_fail(e, "event create");
+    }
+    int rc = CPAB_OK;
+    float bt = 3.0e38f;
+    bool found = false;
+    for (const LaunchShape &c : cands) {
+        rc = run(c);   // warm-up
+        if (rc == kSkip) {
+            rc = CPAB_OK;
+            continue;
+        }
+        if (rc) break;
+        float ms = 3.0e38f;
+        for (int rep = 0; rep < 3 && rc == CPAB_OK; ++rep) {
+            cudaEventRecord(e0, s);
+            rc = run(c);
+            cudaEventRecord(e1, s);
+            cudaError_t e = cudaEventSynchronize(e1);
+            if (e != cudaSuccess) rc = cuda_fail(e, "tuning run");
+            float m = 0.f;
+            if (rc == CPAB_OK && cudaEventElapsedTime(&m, e0, e1) == cudaSuccess && m < ms) ms = m;
+        }
+        if (rc) break;
+        if (ms < bt) {
+            bt = ms;
+            *best = c;
+            found = true;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (!found) return fail(CPAB_ERR_UNSUPPORTED, "no launch shape fits this problem");
+    if (best_ms) *best_ms = bt;
+    return CPAB_OK;
+}
+
+// Tune (or, with force, pin) one kernel family: candidates are timed unless
+// force names the one shape to keep; the kept shape is stored under (kind,
+// key) and run once more to leave its outputs.
+template <typename F>
+int tune_family(int kind, const TuneKey &key, std::vector<LaunchShape> cands,
+                const LaunchShape *force, cudaStream_t s, F run, int *shape, float *best_ms) {
+    LaunchShape best;
+    int rc;
+    if (force) {
+        best = *force;
+        if (best_ms) *best_ms = 0.f;
+    } else if ((rc = time_candidates(cands, s, run, &best, best_ms))) {
+        return rc;
+    }
+    rc = run(best);
+    if (rc == kSkip) return fail(CPAB_ERR_UNSUPPORTED, "the launch shape does not fit this problem");
+    if (rc) return rc;
+    // the run reads the tuner's own workspace, freed when the caller returns
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "tuning run");
+    tuned_set(kind, key, best);
+    put_shape(best, shape);
+    return CPAB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpab_integrate_tune(int ndim, const int *nc, int nsteps, const float *points, int broadcast,
+                        long long nP, const float *E, int n_theta, float *out, const int *force,
+                        int *shape, float *best_ms, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if (nP <= 0 || n_theta <= 0) return fail(CPAB_ERR_ARGUMENT, "nothing to tune (no points)");
+    if ((rc = check_theta_count(n_theta))) return rc;
+    if (!points || !E || !out) return fail(CPAB_ERR_ARGUMENT, "points, E or out is NULL");
+    cudaStream_t s = as_stream(stream);
+    if ((rc = refuse_capture(s, "cpab_integrate_tune"))) return rc;
+    LaunchShape fs;
+    if (force && (rc = check_forward_shape(fs = get_shape(force), 2))) return rc;
+    auto run = [&](const LaunchShape &sh) {
+        return integrate_common(ndim, nc, nsteps, points, broadcast, nP, E, true, n_theta, out,
+                                nullptr, nullptr, stream, &sh);
+    };
+    return tune_family(kTuneIntegrate, tune_key(t, nsteps, 1, nP, n_theta, broadcast ? 1 : 0),
+                       forward_candidates(2), force ? &fs : nullptr, s, run, shape, best_ms);
+}
+
+int cpab_backward_tune(int ndim, const int *nc, int nsteps, int mode, const float *points,
+                       int broadcast, long long nP, const float *A, const float *E, int n_theta,
+                       const float *basis, int d, const float *grad_out, float *dtheta,
+                       float *dpoints, const int *force, int *shape, float *best_ms,
+                       void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if (!grad_mode_ok(mode)) return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
+    if (nP <= 0 || n_theta <= 0 || d < 0 || (d == 0 && !dpoints))
+        return fail(CPAB_ERR_ARGUMENT, "nothing to tune (no points or no outputs)");
+    if ((rc = check_theta_count(n_theta))) return rc;
+    cudaStream_t s = as_stream(stream);
+    if ((rc = refuse_capture(s, "cpab_backward_tune"))) return rc;
+    LaunchShape fs;
+    if (force && (rc = check_adjoint_shape(fs = get_shape(force), ndim))) return rc;
+    auto plan = [&](const LaunchShape &sh, AdjointPlan *pl) {
+        return plan_adjoint(t, nsteps, nP, n_theta, pl, true, &sh);
+    };
+    size_t ws_max = 0;
+    std::vector<LaunchShape> cands = adjoint_candidates(ndim, plan, &ws_max);
+    if (force) {
+        AdjointPlan pl;
+        if (!plan(fs, &pl))
+            return fail(CPAB_ERR_UNSUPPORTED, "the launch shape does not fit this problem");
+        ws_max = pl.ws_floats() * sizeof(float);
+    }
+    Scratch ws;
+    if ((rc = ws.reserve(ws_max))) return rc;
+    auto run = [&](const LaunchShape &sh) {
+        return backward_impl(ndim, nc, nsteps, mode, points, broadcast, nP, A, E, n_theta, basis,
+                             d, grad_out, dtheta, dpoints, ws.p, ws.bytes, nullptr, stream, &sh);
+    };
+    return tune_family(kTuneAdjoint, tune_key(t, nsteps, 0, nP, n_theta, 0), cands,
+                       force ? &fs : nullptr, s, run, shape, best_ms);
+}
+
+int cpab_transform_data_tune(int ndim, const int *nc, int nsteps, const float *lin,
+                             const int *outsize, const float *E, int nb, const float *data, int C,
+                             const int *size, float *out, float *grid_out, const int *force,
+                             int *shape, float *best_ms, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if ((rc = check_geo(ndim, size, outsize, nb))) return rc;
+    if (nb <= 0 || C < 1) return fail(CPAB_ERR_ARGUMENT, "nothing to tune (nb < 1 or C < 1)");
+    cudaStream_t s = as_stream(stream);
+    if ((rc = refuse_capture(s, "cpab_transform_data_tune"))) return rc;
+    LaunchShape fs;
+    if (force && (rc = check_forward_shape(fs = get_shape(force), 2))) return rc;
+    long long nP = 1;
+    for (int j = 0; j < ndim; ++j) nP *= outsize[j];
+    auto run = [&](const LaunchShape &sh) {
+        return td_forward(ndim, nc, nsteps, lin, outsize, E, nb, data, C, size, out, grid_out,
+                          nullptr, stream, &sh);
+    };
+    return tune_family(kTuneFusedForward, tune_key(t, nsteps, 0, nP, nb, C),
+                       forward_candidates(2), force ? &fs : nullptr, s, run, shape, best_ms);
+}
+
+int cpab_transform_data_backward_tune(int ndim, const int *nc, int nsteps, int mode,
+                                      const float *lin, const int *outsize, const float *A,
+                                      const float *E, const float *grid_saved, int nb,
+                                      const float *data, int C, const int *size,
+                                      const float *basis, int d, const float *grad_out,
+                                      float *ddata, float *dtheta, const int *force, int *shape,
+                                      float *best_ms, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if ((rc = check_steps(nsteps))) return rc;
+    if ((rc = check_geo(ndim, size, outsize, nb))) return rc;
+    if (!grad_mode_ok(mode)) return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
+    if (nb <= 0 || C < 1 || d < 0) return fail(CPAB_ERR_ARGUMENT, "nothing to tune (nb < 1)");
+    cudaStream_t s = as_stream(stream);
+    if ((rc = refuse_capture(s, "cpab_transform_data_backward_tune"))) return rc;
+    LaunchShape fs;
+    if (force && (rc = check_adjoint_shape(fs = get_shape(force), ndim))) return rc;
+    long long nP = 1;
+    for (int j = 0; j < ndim; ++j) nP *= outsize[j];
+    auto plan = [&](const LaunchShape &sh, AdjointPlan *pl) {
+        return plan_transform_data_backward(t, nsteps, mode, nP, nb, pl, &sh);
+    };
+    size_t ws_max = 0;
+    std::vector<LaunchShape> cands = adjoint_candidates(ndim, plan, &ws_max);
+    if (force) {
+        AdjointPlan pl;
+        if (!plan(fs, &pl))
+            return fail(CPAB_ERR_UNSUPPORTED, "the launch shape does not fit this problem");
+        ws_max = pl.ws_floats() * sizeof(float);
+    }
+    Scratch ws;
+    if ((rc = ws.reserve(ws_max))) return rc;
+    auto run = [&](const LaunchShape &sh) {
+        return td_backward(ndim, nc, nsteps, mode, lin, outsize, A, E, grid_saved, nb, data, C,
+                           size, basis, d, grad_out, ddata, dtheta, ws.p, ws.bytes, nullptr,
+                           stream, nullptr, &sh);
+    };
+    return tune_family(kTuneFusedBackward, tune_key(t, nsteps, mode, nP, nb, 0), cands,
+                       force ? &fs : nullptr, s, run, shape, best_ms);
+}
+
+int cpab_ragged_points_tune(int kind, int ndim, const int *nc, int nsteps, int mode,
+                            const float *A, const float *E, int S, const long long *offsets,
+                            long long total, const float *basis, int d, const float *points,
+                            const float *grad_out, float *out, float *dtheta, float *dpoints,
+                            const int *force, int *shape, float *best_ms, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if (kind != 0 && kind != 1)
+        return fail(CPAB_ERR_ARGUMENT, "kind must be 0 (forward) or 1 (backward)");
+    if (!grad_mode_ok(mode)) return fail(CPAB_ERR_ARGUMENT, "unknown gradient mode %d", mode);
+    if (S <= 0 || total <= 0) return fail(CPAB_ERR_ARGUMENT, "nothing to tune (no points)");
+    cudaStream_t s = as_stream(stream);
+    if ((rc = refuse_capture(s, "cpab_ragged_points_tune"))) return rc;
+    LaunchShape fs;
+    if (force) {
+        fs = get_shape(force);
+        if (kind == 0 && (rc = check_forward_shape(fs, 4))) return rc;
+        if (kind == 1 && fs.block != 64 && fs.block != 128 && fs.block != 256)
+            return fail(CPAB_ERR_ARGUMENT, "backward launch shape: threads 64, 128 or 256");
+    }
+    Scratch ws;
+    if ((rc = ws.reserve(ragged_points_workspace_bytes(t, S)))) return rc;
+    if (kind == 0) {
+        auto run = [&](const LaunchShape &sh) {
+            return points_forward_impl(ndim, nc, nsteps, E, S, offsets, total, points, out, ws.p,
+                                       ws.bytes, nullptr, stream, &sh);
+        };
+        return tune_family(kTunePointsForward, tune_key(t, nsteps, 0, S, total, 0),
+                           forward_candidates(4), force ? &fs : nullptr, s, run, shape, best_ms);
+    }
+    std::vector<LaunchShape> cands;
+    for (int b : {64, 128, 256}) {
+        LaunchShape sh;
+        sh.block = b;
+        cands.push_back(sh);
+    }
+    auto run = [&](const LaunchShape &sh) {
+        int r = points_backward_impl(ndim, nc, nsteps, mode, A, E, S, offsets, total, basis, d,
+                                     points, grad_out, dtheta, dpoints, ws.p, ws.bytes, nullptr,
+                                     stream, &sh);
+        // a block whose shared memory does not fit is skipped (the launcher
+        // reports it as an unsupported configuration before any launch)
+        return r == CPAB_ERR_UNSUPPORTED ? kSkip : r;
+    };
+    return tune_family(kTunePointsBackward, tune_key(t, nsteps, mode, S, total, 0), cands,
+                       force ? &fs : nullptr, s, run, shape, best_ms);
+}
+
+void cpab_tune_reset(void) { tuned_clear(); }
 
 }  // extern "C"

@@ -129,12 +129,24 @@ cudaError_t launch_sample_grid(int ndim, const float *grid, int nb, const float 
 cudaError_t launch_transform_data(const Tess &t, int nsteps, const float *lin, const int *outsize,
                                   const float *E, int nb, const float *data, int C,
                                   const int *size, float *out, float *grid_out,
-                                  unsigned long long *ties, unsigned *err, cudaStream_t s) {
+                                  unsigned long long *ties, unsigned *err, cudaStream_t s,
+                                  const LaunchShape *force) {
     const Geo g = make_geo(t.ndim, size, outsize);
     if ((long long)nb * g.nP == 0) return cudaSuccess;
-    const int block = 256;
-    const bool two = (long long)nb * g.nP >= (long long)num_sms() * 2048 * 2;
-    const int ppt = two ? 2 : 1;
+    // Default: 256 threads, two points per thread once there is enough work
+    // to fill the GPU twice; or the autotuned / forced shape.
+    LaunchShape sh;
+    if (force) {
+        sh = *force;
+    } else if (!tuned_get(kTuneFusedForward, tune_key(t, nsteps, 0, g.nP, nb, C), &sh)) {
+        sh.block = 256;
+        sh.ppt = (long long)nb * g.nP >= (long long)num_sms() * 2048 * 2 ? 2 : 1;
+    }
+    if (sh.block < 32 || sh.block > 256 || sh.block % 32 || (sh.ppt != 1 && sh.ppt != 2))
+        return cudaErrorInvalidConfiguration;
+    const int block = sh.block;
+    const bool two = sh.ppt == 2;
+    const int ppt = sh.ppt;
     const long long per = (long long)block * ppt;
     const int tiles = (int)((g.nP + per - 1) / per);
     if (nb > 65535) return cudaErrorInvalidConfiguration;   // images on grid y
@@ -223,7 +235,8 @@ __global__ void __launch_bounds__(256)
 }
 
 template <int N, int MODE, typename CT>
-static bool plan_td_t(const Tess &t, int nsteps, long long nP, int nb, AdjointPlan *plan) {
+static bool plan_td_t(const Tess &t, int nsteps, long long nP, int nb, AdjointPlan *plan,
+                      const LaunchShape &sh) {
     int block = 0, per_sm = 0;
     bool global_gw = false;
     size_t smem = 0;
@@ -231,11 +244,11 @@ static bool plan_td_t(const Tess &t, int nsteps, long long nP, int nb, AdjointPl
     decltype(&k_transform_data_backward<N, MODE, CT, false>) kg = nullptr;
     if constexpr (N >= 2) kg = k_transform_data_backward<N, MODE, CT, true>;
     if (!adjoint_shape<N, CT>(k_transform_data_backward<N, MODE, CT, false>, kg, t.nC, nsteps,
-                              &block, &global_gw, &smem, &per_sm))
+                              &block, &global_gw, &smem, &per_sm, sh.block, sh.staging))
         return false;
     const long long tiles = (nP + block - 1) / block;
     const long long target = 2ll * num_sms() * per_sm;
-    long long parts = (target + nb - 1) / nb;
+    long long parts = sh.parts > 0 ? sh.parts : (target + nb - 1) / nb;
     if (parts > tiles) parts = tiles;
     if (parts < 1) parts = 1;
     plan->block = block;
@@ -249,14 +262,14 @@ static bool plan_td_t(const Tess &t, int nsteps, long long nP, int nb, AdjointPl
 }
 
 static bool plan_td_uncached(const Tess &t, int nsteps, int mode, long long nP, int nb,
-                             AdjointPlan *plan) {
+                             AdjointPlan *plan, const LaunchShape &sh) {
     const bool small = t.nC <= 256;
-#define CPAB_PLAN(N)                                                                          \
-    if (mode != 1)                                                                            \
-        return small ? plan_td_t<N, 0, uint8_t>(t, nsteps, nP, nb, plan)                      \
-                     : plan_td_t<N, 0, uint16_t>(t, nsteps, nP, nb, plan);                    \
-    return small ? plan_td_t<N, 1, uint8_t>(t, nsteps, nP, nb, plan)                          \
-                 : plan_td_t<N, 1, uint16_t>(t, nsteps, nP, nb, plan);
+#define CPAB_PLAN(N)                                                                               \
+    if (mode != 1)                                                                                 \
+        return small ? plan_td_t<N, 0, uint8_t>(t, nsteps, nP, nb, plan, sh)                       \
+                     : plan_td_t<N, 0, uint16_t>(t, nsteps, nP, nb, plan, sh);                     \
+    return small ? plan_td_t<N, 1, uint8_t>(t, nsteps, nP, nb, plan, sh)                           \
+                 : plan_td_t<N, 1, uint16_t>(t, nsteps, nP, nb, plan, sh);
     switch (t.ndim) {
         case 1: { CPAB_PLAN(1) }
         case 2: { CPAB_PLAN(2) }
@@ -266,10 +279,15 @@ static bool plan_td_uncached(const Tess &t, int nsteps, int mode, long long nP, 
 }
 
 bool plan_transform_data_backward(const Tess &t, int nsteps, int mode, long long nP, int nb,
-                                  AdjointPlan *plan) {
+                                  AdjointPlan *plan, const LaunchShape *force) {
+    LaunchShape sh;
+    if (force) return plan_td_uncached(t, nsteps, mode, nP, nb, plan, *force);
+    const bool tuned = tuned_get(kTuneFusedBackward, tune_key(t, nsteps, mode, nP, nb, 0), &sh);
+    // the cache key carries the tuned shape (0: the planner's own)
+    const int flag = tuned ? 1 + (sh.staging + 1) + 4 * (sh.block / 32) + 64 * sh.parts : 0;
     static PlanCache cache;
-    return cache.get(1, t, nsteps, mode, nP, nb, 0, plan, [&](AdjointPlan *p) {
-        return plan_td_uncached(t, nsteps, mode, nP, nb, p);
+    return cache.get(1, t, nsteps, mode, nP, nb, flag, plan, [&](AdjointPlan *p) {
+        return plan_td_uncached(t, nsteps, mode, nP, nb, p, sh);
     });
 }
 

@@ -15,6 +15,8 @@
 //     p <- T [p;1] when handed the reference's T tables);
 //   * structure-of-arrays point I/O, coalesced along the point index.
 #include <atomic>
+#include <map>
+#include <mutex>
 
 #include "cpab_launch.h"
 
@@ -69,8 +71,8 @@ template <int N, bool COMP, int PPT>
 static cudaError_t launch_integrate_t(const Tess &t, int nsteps, const float *points,
                                       int broadcast, long long nP, const float *table,
                                       int n_theta, float *out, int *trace,
-                                      unsigned long long *ties, unsigned *err, cudaStream_t s) {
-    constexpr int block = 256;
+                                      unsigned long long *ties, unsigned *err, cudaStream_t s,
+                                      int block) {
     const long long per = (long long)block * PPT;
     const int tiles = (int)((nP + per - 1) / per);
     if ((long long)tiles * n_theta == 0) return cudaSuccess;
@@ -91,19 +93,31 @@ static cudaError_t launch_integrate_t(const Tess &t, int nsteps, const float *po
 cudaError_t launch_integrate(const Tess &t, int nsteps, const float *points, int broadcast,
                              long long nP, const float *table, bool compensated, int n_theta,
                              float *out, int *trace, unsigned long long *ties, unsigned *err,
-                             cudaStream_t s) {
-    // Two points per thread once there is enough work to fill the GPU twice.
-    const bool two = (long long)n_theta * nP >= (long long)num_sms() * 2048 * 2;
-#define CPAB_INTEGRATE(N)                                                                        \
-    if (compensated)                                                                             \
-        return two ? launch_integrate_t<N, true, 2>(t, nsteps, points, broadcast, nP, table,    \
-                                                    n_theta, out, trace, ties, err, s)                  \
-                   : launch_integrate_t<N, true, 1>(t, nsteps, points, broadcast, nP, table,    \
-                                                    n_theta, out, trace, ties, err, s);                 \
-    return two ? launch_integrate_t<N, false, 2>(t, nsteps, points, broadcast, nP, table,       \
-                                                 n_theta, out, trace, ties, err, s)                     \
-               : launch_integrate_t<N, false, 1>(t, nsteps, points, broadcast, nP, table,       \
-                                                 n_theta, out, trace, ties, err, s);
+                             cudaStream_t s, const LaunchShape *force) {
+    // Default: 256 threads, two points per thread once there is enough work
+    // to fill the GPU twice; or the autotuned / forced shape.
+    LaunchShape sh;
+    if (force) {
+        sh = *force;
+    } else if (!tuned_get(kTuneIntegrate, tune_key(t, nsteps, compensated ? 1 : 0, nP, n_theta,
+                                                   broadcast), &sh)) {
+        sh.block = 256;
+        sh.ppt = (long long)n_theta * nP >= (long long)num_sms() * 2048 * 2 ? 2 : 1;
+    }
+    if (sh.block < 32 || sh.block > 256 || sh.block % 32 || (sh.ppt != 1 && sh.ppt != 2))
+        return cudaErrorInvalidConfiguration;
+    const bool two = sh.ppt == 2;
+    const int block = sh.block;
+#define CPAB_INTEGRATE(N)                                                                          \
+    if (compensated)                                                                               \
+        return two ? launch_integrate_t<N, true, 2>(t, nsteps, points, broadcast, nP, table,       \
+                                                    n_theta, out, trace, ties, err, s, block)      \
+                   : launch_integrate_t<N, true, 1>(t, nsteps, points, broadcast, nP, table,       \
+                                                    n_theta, out, trace, ties, err, s, block);     \
+    return two ? launch_integrate_t<N, false, 2>(t, nsteps, points, broadcast, nP, table,          \
+                                                 n_theta, out, trace, ties, err, s, block)         \
+               : launch_integrate_t<N, false, 1>(t, nsteps, points, broadcast, nP, table,          \
+                                                 n_theta, out, trace, ties, err, s, block);
     switch (t.ndim) {
         case 1: { CPAB_INTEGRATE(1) }
         case 2: { CPAB_INTEGRATE(2) }
@@ -134,6 +148,49 @@ cudaError_t launch_findcellidx(const Tess &t, const float *points, long long nP,
         default: k_findcellidx<3><<<grid, block, 0, s>>>(t, points, nP, out, ties); break;
     }
     return cudaGetLastError();
+}
+
+// ---------------------------- tuned launch shapes ----------------------------
+namespace {
+std::mutex g_shape_mu;
+std::map<std::pair<int, std::array<long long, 10>>, LaunchShape> g_shapes;
+}  // namespace
+
+TuneKey tune_key(const Tess &t, int nsteps, int mode, long long a, long long b, long long c) {
+    return TuneKey{t.ndim, t.nc[0], t.nc[1], t.nc[2], (long long)nsteps * 4 + mode, a, b, c};
+}
+
+static std::array<long long, 10> full_key(const TuneKey &k) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        dev = 0;
+    }
+    std::array<long long, 10> f{};
+    f[0] = dev;
+    for (int i = 0; i < 8; ++i) f[i + 1] = k[i];
+    return f;
+}
+
+bool tuned_get(int kind, const TuneKey &key, LaunchShape *shape) {
+    const auto k = std::make_pair(kind, full_key(key));
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    auto it = g_shapes.find(k);
+    if (it == g_shapes.end()) return false;
+    *shape = it->second;
+    return true;
+}
+
+void tuned_set(int kind, const TuneKey &key, const LaunchShape &shape) {
+    const auto k = std::make_pair(kind, full_key(key));
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    if (g_shapes.size() > 4096) g_shapes.clear();
+    g_shapes[k] = shape;
+}
+
+void tuned_clear() {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    g_shapes.clear();
 }
 
 // SM count of the current device, looked up once per device (relaxed atomics:

@@ -5,9 +5,38 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <array>
+
 #include "cpab_common.cuh"
 
 namespace cpab {
+
+// ------------------------------- autotuner ----------------------------------
+// Launch shapes picked by the autotuner entry points (cpab_integrate_tune,
+// cpab_transform_data_tune, cpab_ragged_points_tune), cached per device,
+// kernel family and problem shape.  A launcher takes the cached shape when
+// there is one and its own heuristic otherwise; `force` (the candidates the
+// tuner times) overrides both.  Fields left at their defaults mean "the
+// heuristic's choice".
+struct LaunchShape {
+    int block = 0;      // threads per CTA
+    int ppt = 0;        // points per thread (forward kernels)
+    int parts = 0;      // CTAs per theta or image (fused backward)
+    int staging = -1;   // fused backward: per-warp tables in shared (0) / global (1) memory
+};
+enum TuneKind : int {
+    kTuneIntegrate = 1,
+    kTuneFusedForward = 2,
+    kTuneFusedBackward = 3,
+    kTunePointsForward = 4,
+    kTunePointsBackward = 5,
+    kTuneAdjoint = 6
+};
+using TuneKey = std::array<long long, 8>;
+TuneKey tune_key(const Tess &t, int nsteps, int mode, long long a, long long b, long long c);
+bool tuned_get(int kind, const TuneKey &key, LaunchShape *shape);
+void tuned_set(int kind, const TuneKey &key, const LaunchShape &shape);
+void tuned_clear();
 
 // Per-(theta, cell) tables from theta and the basis B [D, d] (fp32):
 // A = B theta, T = expm(dt [A;0]) (rows 0..ndim-1), E = T - I.
@@ -21,7 +50,7 @@ cudaError_t launch_cell_tables(const Tess &t, int nsteps, const float *theta, in
 cudaError_t launch_integrate(const Tess &t, int nsteps, const float *points, int broadcast,
                              long long nP, const float *table, bool compensated, int n_theta,
                              float *out, int *trace, unsigned long long *ties, unsigned *err,
-                             cudaStream_t s);
+                             cudaStream_t s, const LaunchShape *force = nullptr);
 
 cudaError_t launch_findcellidx(const Tess &t, const float *points, long long nP, int *out,
                                unsigned long long *ties, cudaStream_t s);
@@ -46,9 +75,10 @@ struct AdjointPlan {
     size_t ws_floats() const { return gw_floats ? gw_offset() + gw_floats : partial_floats; }
 };
 bool plan_adjoint(const Tess &t, int nsteps, long long nP, int n_theta, AdjointPlan *plan,
-                  bool allow_global_gw = true);
+                  bool allow_global_gw = true, const LaunchShape *force = nullptr);
 bool plan_adjoint_mode(const Tess &t, int nsteps, int mode, long long nP, int n_theta,
-                       AdjointPlan *plan, bool allow_global_gw = true);
+                       AdjointPlan *plan, bool allow_global_gw = true,
+                       const LaunchShape *force = nullptr);
 cudaError_t launch_adjoint(const Tess &t, int nsteps, int mode, const AdjointPlan &plan,
                            const float *points, int broadcast, long long nP, const float *table,
                            int n_theta, const float *gout, float *dpoints, float *partials,
@@ -76,10 +106,11 @@ cudaError_t launch_interpolate_backward(int ndim, const float *data, int nb, int
 cudaError_t launch_transform_data(const Tess &t, int nsteps, const float *lin, const int *outsize,
                                   const float *E, int nb, const float *data, int C,
                                   const int *size, float *out, float *grid_out,
-                                  unsigned long long *ties, unsigned *err, cudaStream_t s);
+                                  unsigned long long *ties, unsigned *err, cudaStream_t s,
+                                  const LaunchShape *force = nullptr);
 
 bool plan_transform_data_backward(const Tess &t, int nsteps, int mode, long long nP, int nb,
-                                  AdjointPlan *plan);
+                                  AdjointPlan *plan, const LaunchShape *force = nullptr);
 
 // Transformations applied to the grid before the one being differentiated
 // (a composition T_K o ... o T_1 differentiated in theta_K only): their
@@ -169,14 +200,16 @@ size_t ragged_points_workspace_bytes(const Tess &t, int S);
 cudaError_t launch_ragged_points_forward(const Tess &t, int nsteps, int S, const long long *off,
                                          long long total, const float *E, const float *points,
                                          float *out, void *ws, unsigned long long *ties,
-                                         unsigned *err, cudaStream_t s);
+                                         unsigned *err, cudaStream_t s,
+                                         const LaunchShape *force = nullptr);
 cudaError_t launch_ragged_points_backward(const Tess &t, int nsteps, int mode, int S,
                                           const long long *off, long long total, const float *A,
                                           const float *E, const float *points,
                                           const float *gout, float *dpoints, const float *basis,
                                           int d, float *dtheta, void *ws,
                                           unsigned long long *ties, unsigned *err,
-                                          cudaStream_t s);
+                                          cudaStream_t s,
+                                          const LaunchShape *force = nullptr);
 
 cudaError_t launch_sample_grid(int ndim, const float *grid, int nb, const float *data, int C,
                                const int *size, const int *outsize, float *out, cudaStream_t s);

@@ -197,9 +197,8 @@ template <int N, int PPT>
 static cudaError_t launch_rpf_t(const Tess &t, int nsteps, int S, const long long *off,
                                 const int *tile_off, const float *E, long long total,
                                 const float *points, float *out, unsigned long long *ties,
-                                unsigned *err, cudaStream_t s) {
+                                unsigned *err, cudaStream_t s, int block) {
     auto kern = k_ragged_points_forward<N, PPT>;
-    const int block = 256;
     const size_t smem = (size_t)(block / 32) * round4(t.nC * N * (N + 1)) * 4;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -214,35 +213,60 @@ static cudaError_t launch_rpf_t(const Tess &t, int nsteps, int S, const long lon
     return cudaGetLastError();
 }
 
+template <int N>
+static cudaError_t launch_rpf_n(int ppt, const Tess &t, int nsteps, int S, const long long *off,
+                                const int *tile_off, const float *E, long long total,
+                                const float *points, float *out, unsigned long long *ties,
+                                unsigned *err, cudaStream_t s, int block) {
+    switch (ppt) {
+        case 1: return launch_rpf_t<N, 1>(t, nsteps, S, off, tile_off, E, total, points, out, ties, err, s, block);
+        case 2: return launch_rpf_t<N, 2>(t, nsteps, S, off, tile_off, E, total, points, out, ties, err, s, block);
+        default: return launch_rpf_t<N, 4>(t, nsteps, S, off, tile_off, E, total, points, out, ties, err, s, block);
+    }
+}
+
 cudaError_t launch_ragged_points_forward(const Tess &t, int nsteps, int S, const long long *off,
                                          long long total, const float *E, const float *points,
                                          float *out, void *ws, unsigned long long *ties,
-                                         unsigned *err, cudaStream_t s) {
+                                         unsigned *err, cudaStream_t s, const LaunchShape *force) {
     int *tile_off;
     float *partials;
     points_carve(S, ws, &tile_off, &partials);
     if (S == 0) return cudaSuccess;
-    const int ppt = 2;
-    cudaError_t e = launch_ragged_plan(S, off, total, 32 * ppt, tile_off, err, s);
+    // Default: 256 threads, 2 points per lane; or the autotuned / forced shape.
+    LaunchShape sh;
+    if (force) {
+        sh = *force;
+    } else if (!tuned_get(kTunePointsForward, tune_key(t, nsteps, 0, S, total, 0), &sh)) {
+        sh.block = 256;
+        sh.ppt = 2;
+    }
+    if (sh.block < 32 || sh.block > 256 || sh.block % 32 ||
+        (sh.ppt != 1 && sh.ppt != 2 && sh.ppt != 4))
+        return cudaErrorInvalidConfiguration;
+    cudaError_t e = launch_ragged_plan(S, off, total, 32 * sh.ppt, tile_off, err, s);
     if (e != cudaSuccess) return e;
     switch (t.ndim) {
-        case 1: return launch_rpf_t<1, 2>(t, nsteps, S, off, tile_off, E, total, points, out, ties, err, s);
-        case 2: return launch_rpf_t<2, 2>(t, nsteps, S, off, tile_off, E, total, points, out, ties, err, s);
-        default: return launch_rpf_t<3, 2>(t, nsteps, S, off, tile_off, E, total, points, out, ties, err, s);
+        case 1: return launch_rpf_n<1>(sh.ppt, t, nsteps, S, off, tile_off, E, total, points, out, ties, err, s, sh.block);
+        case 2: return launch_rpf_n<2>(sh.ppt, t, nsteps, S, off, tile_off, E, total, points, out, ties, err, s, sh.block);
+        default: return launch_rpf_n<3>(sh.ppt, t, nsteps, S, off, tile_off, E, total, points, out, ties, err, s, sh.block);
     }
 }
 
 // Largest block size whose shared memory fits (0: none).
+// force_block > 0: that block size if it fits, else 0.
 template <int N, typename CT>
-static int points_block(const Tess &t, int nsteps) {
+static int points_block(const Tess &t, int nsteps, int force_block) {
     int dev = 0, max_optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (max_optin <= 0) max_optin = 48 * 1024;
     const int cands[3] = {256, 128, 64};
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i) {
+        if (force_block > 0 && cands[i] != force_block) continue;
         if (points_adjoint_smem<N, CT>(t.nC, nsteps, cands[i]) <= (size_t)max_optin)
             return cands[i];
+    }
     return 0;
 }
 
@@ -252,8 +276,8 @@ static cudaError_t launch_rpa_t(const Tess &t, int nsteps, int S, const long lon
                                 long long total, const float *points, const float *gout,
                                 float *dpoints, float *partials, const float *basis, int d,
                                 float *dtheta, unsigned long long *ties, unsigned *err,
-                                cudaStream_t s) {
-    const int block = points_block<N, CT>(t, nsteps);
+                                cudaStream_t s, int force_block) {
+    const int block = points_block<N, CT>(t, nsteps, force_block);
     if (!block) return cudaErrorInvalidConfiguration;
     auto kern = k_ragged_points_adjoint<N, MODE, CT>;
     const size_t smem = points_adjoint_smem<N, CT>(t.nC, nsteps, block);
@@ -289,35 +313,43 @@ cudaError_t launch_ragged_points_backward(const Tess &t, int nsteps, int mode, i
                                           const float *gout, float *dpoints, const float *basis,
                                           int d, float *dtheta, void *ws,
                                           unsigned long long *ties, unsigned *err,
-                                          cudaStream_t s) {
+                                          cudaStream_t s, const LaunchShape *force) {
     int *tile_off;
     float *partials;
     points_carve(S, ws, &tile_off, &partials);
     if (S == 0) return cudaSuccess;
+    // Default: the largest block whose shared memory fits; or the autotuned /
+    // forced block size (64, 128 or 256 threads).
+    LaunchShape sh;
+    if (force) sh = *force;
+    else tuned_get(kTunePointsBackward, tune_key(t, nsteps, mode, S, total, 0), &sh);
+    if (sh.block != 0 && sh.block != 64 && sh.block != 128 && sh.block != 256)
+        return cudaErrorInvalidConfiguration;
+    const int fb = sh.block;
     cudaError_t e = launch_ragged_plan(S, off, total, 32, tile_off, err, s);
     if (e != cudaSuccess) return e;
     const bool small = t.nC <= 256;
-#define CPAB_RPA(N)                                                                            \
-    if (mode == 0)                                                                             \
-        return small ? launch_rpa_t<N, 0, uint8_t>(t, nsteps, S, off, tile_off, A, E, total,   \
-                                                   points, gout, dpoints, partials, basis, d,  \
-                                                   dtheta, ties, err, s)                       \
-                     : launch_rpa_t<N, 0, uint16_t>(t, nsteps, S, off, tile_off, A, E, total,  \
-                                                    points, gout, dpoints, partials, basis, d, \
-                                                    dtheta, ties, err, s);                     \
-    if (mode == 2)                                                                             \
-        return small ? launch_rpa_t<N, 2, uint8_t>(t, nsteps, S, off, tile_off, A, E, total,   \
-                                                   points, gout, dpoints, partials, basis, d,  \
-                                                   dtheta, ties, err, s)                       \
-                     : launch_rpa_t<N, 2, uint16_t>(t, nsteps, S, off, tile_off, A, E, total,  \
-                                                    points, gout, dpoints, partials, basis, d, \
-                                                    dtheta, ties, err, s);                     \
-    return small ? launch_rpa_t<N, 1, uint8_t>(t, nsteps, S, off, tile_off, A, E, total, points, \
-                                               gout, dpoints, partials, basis, d, dtheta, ties, \
-                                               err, s)                                          \
-                 : launch_rpa_t<N, 1, uint16_t>(t, nsteps, S, off, tile_off, A, E, total,       \
-                                                points, gout, dpoints, partials, basis, d,      \
-                                                dtheta, ties, err, s);
+#define CPAB_RPA(N)                                                                                \
+    if (mode == 0)                                                                                 \
+        return small ? launch_rpa_t<N, 0, uint8_t>(t, nsteps, S, off, tile_off, A, E, total,       \
+                                                   points, gout, dpoints, partials, basis, d,      \
+                                                   dtheta, ties, err, s, fb)                       \
+                     : launch_rpa_t<N, 0, uint16_t>(t, nsteps, S, off, tile_off, A, E, total,      \
+                                                    points, gout, dpoints, partials, basis, d,     \
+                                                    dtheta, ties, err, s, fb);                     \
+    if (mode == 2)                                                                                 \
+        return small ? launch_rpa_t<N, 2, uint8_t>(t, nsteps, S, off, tile_off, A, E, total,       \
+                                                   points, gout, dpoints, partials, basis, d,      \
+                                                   dtheta, ties, err, s, fb)                       \
+                     : launch_rpa_t<N, 2, uint16_t>(t, nsteps, S, off, tile_off, A, E, total,      \
+                                                    points, gout, dpoints, partials, basis, d,     \
+                                                    dtheta, ties, err, s, fb);                     \
+    return small ? launch_rpa_t<N, 1, uint8_t>(t, nsteps, S, off, tile_off, A, E, total, points,   \
+                                               gout, dpoints, partials, basis, d, dtheta, ties,    \
+                                               err, s, fb)                                         \
+                 : launch_rpa_t<N, 1, uint16_t>(t, nsteps, S, off, tile_off, A, E, total,          \
+                                                points, gout, dpoints, partials, basis, d,         \
+                                                dtheta, ties, err, s, fb);
     switch (t.ndim) {
         case 1: { CPAB_RPA(1) }
         case 2: { CPAB_RPA(2) }
