@@ -12,7 +12,11 @@ One step = forward + backward of that loss over the whole batch
 Under torchrun (N > 1) every rank runs the full batch with its own seeds
 (weak scaling, no data-path collective); the slowest rank's time sets the
 aggregate.  --impl reference times the reference's CPU implementation of the
-same step (the C oracle port, all host threads) on a bounded sample.
+same step (its compiled libcpab/core/cpab_ops.cpp op, all host threads; the C
+restatement only where that build is missing) on a bounded sample.  Beside the
+headline the line carries the reference's own GPU path on the same inputs
+(plain_gpu_reference), the timed step's error against the FP64 oracle
+(error_vs_fp64), the autotuned launch shapes and the other workloads' legs.
 """
 import argparse
 import json
@@ -38,14 +42,14 @@ L2_BYTES = 129 * 2 ** 20
 # algorithmic work per point trajectory (2D, 50 steps): forward 17 flop/step,
 # adjoint 37 flop/step; interpolation 8*C bytes (forward), 12*C (backward)
 FLOP_FWD_STEP, FLOP_ADJ_STEP = 17, 37
-# thread instructions per point-step of the fused kernels (2D [3,3]), from the
-# ncu capture of 16 images summarised in profiles/ (smsp__inst_executed x
-# active threads per instruction / point-steps)
-INSTR_FWD_STEP, INSTR_BWD_STEP = 73, 159
+# thread instructions per point-step of the fused kernels (2D [3,3], reference
+# gradient), from the ncu capture of 16 images summarised in profiles/
+# (smsp__inst_executed x active threads per instruction / point-steps)
+INSTR_FWD_STEP, INSTR_BWD_STEP = 73, 216
 # DRAM bytes (read + write) of one k_transform_data_backward launch per image,
-# from an ncu capture of 16 images (36.06 MB); traffic grows with the images
+# from an ncu capture of 16 images (36.26 MB); traffic grows with the images
 # processed
-BWD_DRAM_BYTES_PER_IMAGE = 36.06e6 / 16
+BWD_DRAM_BYTES_PER_IMAGE = 36.26e6 / 16
 
 
 def parse():
