@@ -405,7 +405,10 @@ def run_gb300(args):
     fwd_ms = sum(t_fwd) / len(t_fwd)
     bwd_flop = pts * NSTEPS * (FLOP_FWD_STEP + FLOP_ADJ_STEP)
     sm_mhz = clk['sm_mhz'] if clk else 2070.0
-    fp32_peak = 152 * 128 * 2 * 2070e6 / 1e12        # TFLOP/s at the maximum SM clock
+    sm_max = clk['sm_max_mhz'] if clk and clk.get('sm_max_mhz') else 2070.0
+    n_sm = torch.cuda.get_device_properties(device).multi_processor_count
+    fp32_peak = n_sm * 128 * 2 * sm_max * 1e6 / 1e12   # TFLOP/s at the maximum SM clock
+    issue_peak = n_sm * 4 * sm_mhz * 1e6                # warp instructions/s at the sampled clock
     achieved = bwd_flop / (bwd_ms / 1e3) / 1e12
     fwd_bytes = pts * 8 * CHANNELS
     result = None
@@ -435,8 +438,9 @@ def run_gb300(args):
             'roofline': {'bound': 'fp32', 'kernel': 'k_transform_data_backward (+finalize)',
                          'achieved': achieved, 'peak': fp32_peak, 'unit': 'TFLOP/s',
                          'frac': achieved / fp32_peak,
-                         'peak_source': 'derived: 152 SM x 128 FP32 lanes x 2 flop x 2070 MHz '
-                                        '(MEASURED_PEAKS has HBM and bf16 only)',
+                         'peak_source': 'derived: %d SMs x 128 FP32 lanes x 2 flop x %.0f MHz '
+                                        '(MEASURED_PEAKS has HBM and bf16 only)'
+                                        % (n_sm, sm_max),
                          'flop_per_launch': bwd_flop, 'ms_per_launch': bwd_ms,
                          'traffic': BWD_DRAM_BYTES_PER_IMAGE * args.batch,
                          'traffic_unit': 'bytes per launch (ncu dram read+write, 16-image '
@@ -447,15 +451,13 @@ def run_gb300(args):
                          'FP32/integer work, not FMA streams)',
                 'warp_instr_per_launch': pts * NSTEPS * INSTR_BWD_STEP / 32,
                 'achieved': pts * NSTEPS * INSTR_BWD_STEP / 32 / (bwd_ms / 1e3),
-                'peak': 152 * 4 * sm_mhz * 1e6,
+                'peak': issue_peak,
                 'unit': 'warp instructions/s',
-                'frac': pts * NSTEPS * INSTR_BWD_STEP / 32 / (bwd_ms / 1e3)
-                        / (152 * 4 * sm_mhz * 1e6),
-                'forward_frac': pts * NSTEPS * INSTR_FWD_STEP / 32 / (fwd_ms / 1e3)
-                                / (152 * 4 * sm_mhz * 1e6),
+                'frac': pts * NSTEPS * INSTR_BWD_STEP / 32 / (bwd_ms / 1e3) / issue_peak,
+                'forward_frac': pts * NSTEPS * INSTR_FWD_STEP / 32 / (fwd_ms / 1e3) / issue_peak,
                 'source': 'instructions per point-step from ncu (%d bwd, %d fwd); peak = '
-                          '152 SMs x 4 schedulers x 1 instruction/cycle at the sampled SM '
-                          'clock' % (INSTR_BWD_STEP, INSTR_FWD_STEP)},
+                          '%d SMs x 4 schedulers x 1 instruction/cycle at the sampled SM '
+                          'clock' % (INSTR_BWD_STEP, INSTR_FWD_STEP, n_sm)},
             'launch_shapes': shapes,
             'backward_ms_per_launch_by_gradient_mode': {
                 'reference': bwd_ms,

@@ -267,3 +267,64 @@ def test_rank_time_reduction_gloo():
         p.join(60)
     res = dict(q.get(timeout=5) for _ in range(2))
     assert res[0] == res[1] == [2.0, 5.0]
+
+
+def _shard_main(rank, world, port, q):
+    """One rank of a theta-sharded step: this rank's theta rows of the golden
+    2D [3,3] problem through the oracle's reference forward and analytic
+    gradient, then the shards gathered over gloo."""
+    import torch
+    import torch.distributed as dist
+    os.environ['MASTER_ADDR'] = '127.0.0.1'
+    os.environ['MASTER_PORT'] = str(port)
+    dist.init_process_group('gloo', rank=rank, world_size=world)
+    from oracle.oracle import Oracle
+    out, dth = _shard_step(Oracle(), rank, world)
+    outs = [torch.zeros_like(out) for _ in range(world)]
+    dths = [torch.zeros_like(dth) for _ in range(world)]
+    dist.all_gather(outs, out)
+    dist.all_gather(dths, dth)
+    if rank == 0:
+        q.put((torch.cat(outs).numpy(), torch.cat(dths).numpy()))
+    dist.destroy_process_group()
+
+
+def _shard_step(orc, rank, world):
+    """Rows rank*n/world .. (rank+1)*n/world of theta (contiguous shards of
+    equal size): forward with the reference step maps and the reference's
+    analytic gradient for a fixed cotangent."""
+    import torch
+    g = load_golden('2d_3x3_zb')
+    n = g['theta'].shape[0]
+    assert n % world == 0
+    lo, hi = rank * n // world, (rank + 1) * n // world
+    nc = [int(x) for x in g['nc']]
+    out = orc.forward(nc, 50, g['grid'], g['trels_ref'][lo:hi])
+    d = g['B'].shape[1]
+    Bs = np.asarray(g['B']).T.reshape(d, -1, 2, 3).astype(np.float32)
+    dth = orc.backward(nc, 50, g['grid'], g['As_ref'][lo:hi], Bs, g['cot'][lo:hi])
+    return torch.tensor(np.asarray(out)), torch.tensor(np.asarray(dth))
+
+
+def test_theta_sharded_step_gloo(oracle):
+    """The path shards by theta with no data-path exchange: two gloo ranks,
+    each integrating and differentiating its half of the theta rows, gather
+    exactly the single-process results (every trajectory and its gradient
+    depend on their own theta only)."""
+    import socket
+    import torch.multiprocessing as mp
+    s = socket.socket()
+    s.bind(('127.0.0.1', 0))
+    port = s.getsockname()[1]
+    s.close()
+    ctx = mp.get_context('spawn')
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_shard_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    out2, dth2 = q.get(timeout=120)
+    for p in ps:
+        p.join(60)
+    out1, dth1 = _shard_step(oracle, 0, 1)
+    assert np.array_equal(out2, out1.numpy())
+    assert np.array_equal(dth2, dth1.numpy())

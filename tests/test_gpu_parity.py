@@ -70,6 +70,38 @@ def test_findcellidx_random_vs_oracle(name, cuda, oracle):
 
 
 @pytest.mark.parametrize('name', SMALL)
+def test_cell_tables_vs_reference(name, cuda):
+    """k_cell_tables against the reference's own tables for the same theta:
+    A = B theta (libcpab/pytorch/transformer.py:146-150, an fp32 matmul) and
+    the step maps T = expm(A~ / nsteps) (its fp32 Pade expm,
+    libcpab/pytorch/expm.py:11-55), and E = T - I against FP64.
+    Tolerances: A within 1e-6 of max|A| (fp32 sums in another order); T within
+    1e-6 absolute (two fp32 exponentials, entries near 1); E within 1e-5 of
+    max|E| of the FP64 step maps minus I (the compensated table keeps the
+    increment to full relative precision; T_ref - I loses it to cancellation)."""
+    from libcpab_gb300 import _native as N
+    from oracle.oracle import step_maps_fp64
+    g = load_golden(name)
+    nc = [int(x) for x in g['nc']]
+    ndim = len(nc)
+    B = np.asarray(g['B'], dtype=np.float64)
+    basis = torch.tensor(np.ascontiguousarray(B, dtype=np.float32), device=cuda)
+    theta = torch.tensor(np.ascontiguousarray(g['theta'], dtype=np.float32), device=cuda)
+    A, T, E = N.cell_tables(nc, NSTEPS, theta, basis, want_T=True)
+    A, T, E = A.cpu().numpy(), T.cpu().numpy(), E.cpu().numpy()
+    As_ref = np.asarray(g['As_ref'], dtype=np.float64)
+    assert A.shape == As_ref.shape
+    assert np.abs(A - As_ref).max() <= 1e-6 * max(1.0, np.abs(As_ref).max())
+    assert np.abs(T - g['trels_ref']).max() <= 1e-6
+    if B.shape[1] == 0:
+        assert np.all(E == 0)
+        return
+    T64 = step_maps_fp64(B, np.asarray(g['theta'], dtype=np.float64), ndim, NSTEPS)
+    E64 = T64[:, :, :ndim, :] - np.eye(ndim, ndim + 1)
+    assert np.abs(E - E64).max() <= 1e-5 * max(np.abs(E64).max(), 1e-30)
+
+
+@pytest.mark.parametrize('name', SMALL)
 def test_forward_with_reference_step_maps(name, cuda):
     """cpab_forward fed the reference's own fp32 Pade step maps reproduces the
     reference's pytorch-CPU result; differences come only from FMA rounding
