@@ -937,8 +937,9 @@ def run_aligner(device, iters=100):
 
 def run_exact_flow(device, steps, flush):
     """The opt-in exact-flow scheme on the headline grid (tess [3,3],
-    64 theta ~ N(0, 0.25 I), 224^2 grid): transform_grid forward, against the
-    fixed-step scheme on the same points."""
+    64 theta ~ N(0, 0.25 I), 224^2 grid): transform_grid forward and its
+    dtheta backward (reverse sweep), against the fixed-step scheme on the same
+    points."""
     from libcpab_gb300 import Cpab, _native as N
     from libcpab_gb300.functions import basis_on
     T = Cpab(NC, backend='pytorch', device='gpu', zero_boundary=True)
@@ -955,11 +956,18 @@ def run_exact_flow(device, steps, flush):
     cnt = torch.zeros(1, dtype=torch.int64, device=device)
     ex = N.integrate_exact(NC, grid, A, steps=cnt)
     fs = N.integrate(NC, NSTEPS, grid, E)
+    gout = torch.randn(ex.shape, generator=torch.Generator().manual_seed(5)).to(device)
+    for _ in range(2):
+        N.backward_exact(NC, ex, A, basis, gout)
+    t_bw = time_events(lambda: N.backward_exact(NC, ex, A, basis, gout), max(2, steps // 2),
+                       flush)
     pts = BATCH * SIZE * SIZE
     ms_ex, ms_fs = sum(t_ex) / len(t_ex), sum(t_fs) / len(t_fs)
+    ms_bw = sum(t_bw) / len(t_bw)
     return {'workload': 'transform_grid, tess [3,3] zero_boundary, 64 theta ~ N(0,0.25I), '
                         '224^2 grid',
             'exact_ms': ms_ex, 'exact_points_per_s': pts / (ms_ex / 1e3),
+            'exact_backward_ms': ms_bw,
             'fixed_step_ms': ms_fs, 'in_cell_steps_per_point': int(cnt.item()) / pts,
             'max_abs_diff_exact_vs_fixed_step': float((ex - fs).abs().max())}
 

@@ -5,7 +5,8 @@
  * is a CUDA device pointer to contiguous float32 (or int32) memory on the
  * current device; `nc`, `size` and `outsize` are host arrays of `ndim` ints.
  * `stream` is a cudaStream_t (NULL = legacy default stream).  Work is only
- * enqueued: no entry point synchronises the host except cpab_device_status.
+ * enqueued: no entry point synchronises the host except cpab_device_status
+ * and the autotuners (cpab_*_tune).
  *
  * Every entry point returns CPAB_OK (0) or an error code; the message for
  * the last error of the calling thread is returned by cpab_last_error().
@@ -241,12 +242,32 @@ CPAB_API int cpab_transform_data_backward(int ndim, const int *nc, int nsteps, i
  * continuous piecewise-affine field for time 1.  A: velocity tables
  * [n_theta, nC, ndim, ndim+1] (cpab_cell_tables).  1D in closed form, 2D/3D
  * by certified in-cell steps of the analytic cell flow.  steps (device
- * uint64, may be NULL) accumulates the in-cell steps taken.  Forward only.
+ * uint64, may be NULL) accumulates the in-cell steps taken.  Its gradient:
+ * cpab_backward_exact.
  */
 CPAB_API int cpab_integrate_exact(int ndim, const int *nc, const float *points, int broadcast,
                                   long long nP, const float *A, int n_theta, float *out,
                                   unsigned long long *ties, unsigned long long *steps,
                                   void *stream);
+
+/*
+ * Backward of cpab_integrate_exact (no counterpart in the reference): dtheta
+ * [n_theta, d] (overwritten; deterministic) and dL/dpoints [n_theta, ndim, nP]
+ * (overwritten, may be NULL) from grad_out = dL/d(out), where out
+ * [n_theta, ndim, nP] is cpab_integrate_exact's result for the same A.  The
+ * flow is integrated backwards from out in certified in-cell sub-steps; per
+ * sub-step the cotangent is carried back through the in-cell flow and dL/dA
+ * gathers the adjoint Frechet derivative of its exponential.  The field is
+ * continuous across faces, so the crossing times add no term.  workspace:
+ * cpab_backward_exact_workspace() bytes of device memory.
+ */
+CPAB_API size_t cpab_backward_exact_workspace(int ndim, const int *nc, long long nP,
+                                              int n_theta);
+CPAB_API int cpab_backward_exact(int ndim, const int *nc, const float *out, long long nP,
+                                 const float *A, int n_theta, const float *basis, int d,
+                                 const float *grad_out, float *dtheta, float *dpoints,
+                                 void *workspace, size_t workspace_bytes,
+                                 unsigned long long *ties, void *stream);
 
 /*
  * Composition T_K o ... o T_1 (1 <= K <= 4 transformations of the same ndim):

@@ -61,7 +61,8 @@ class TransformGrid(torch.autograd.Function):
         else:
             A, _, E = N.cell_tables(params.nc, params.nstepsolver, theta_c, basis)
             out = N.integrate(params.nc, params.nstepsolver, points, E, ties=_ties(params))
-        ctx.save_for_backward(points, A, E)
+        # the exact scheme's backward integrates back from its result
+        ctx.save_for_backward(points, A, out if ctx.exact else E)
         ctx.params = params
         ctx.points_dim = points.dim()
         ctx.theta_like = (theta_c.shape, theta_c.dtype, theta_c.device)
@@ -75,9 +76,6 @@ class TransformGrid(torch.autograd.Function):
     def backward(ctx, grad):
         points, A, E = ctx.saved_tensors
         params = ctx.params
-        if ctx.exact:
-            raise NotImplementedError("the 'exact' integration scheme is forward only; use "
-                                      "integration='fixed_step' for gradients")
         if grad is None:
             # the reference computes this gradient from a zero cotangent: zeros
             shape, dtype, dev = ctx.theta_like
@@ -88,10 +86,16 @@ class TransformGrid(torch.autograd.Function):
         want_p = ctx.needs_input_grad[0] and getattr(params, 'point_gradient', False)
         if not (want_p or ctx.needs_input_grad[1]):
             return None, None, None
-        dtheta, dpoints = N.backward(params.nc, params.nstepsolver, _mode(params), points, A, E,
-                                     _basis(params, points.device),
-                                     grad.to(torch.float32).contiguous(),
-                                     want_dpoints=want_p, ties=_ties(params))
+        if ctx.exact:
+            # E holds the forward result here
+            dtheta, dpoints = N.backward_exact(params.nc, E, A, _basis(params, points.device),
+                                               grad.to(torch.float32).contiguous(),
+                                               want_dpoints=want_p, ties=_ties(params))
+        else:
+            dtheta, dpoints = N.backward(params.nc, params.nstepsolver, _mode(params), points, A,
+                                         E, _basis(params, points.device),
+                                         grad.to(torch.float32).contiguous(),
+                                         want_dpoints=want_p, ties=_ties(params))
         if dpoints is not None and ctx.points_dim == 2:
             dpoints = dpoints.sum(dim=0)
         return dpoints, (dtheta if ctx.needs_input_grad[1] else None), None

@@ -35,6 +35,9 @@ _SIGS = {
     'cpab_integrate': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _vp, _vp], _i),
     'cpab_integrate_trace': ([_i, _c_int_p, _i, _vp, _i, _ll, _vp, _i, _vp, _vp, _vp], _i),
     'cpab_integrate_exact': ([_i, _c_int_p, _vp, _i, _ll, _vp, _i, _vp, _vp, _vp, _vp], _i),
+    'cpab_backward_exact_workspace': ([_i, _c_int_p, _ll, _i], _sz),
+    'cpab_backward_exact': ([_i, _c_int_p, _vp, _ll, _vp, _i, _vp, _i, _vp, _vp, _vp, _vp, _sz,
+                             _vp, _vp], _i),
     'cpab_backward_workspace': ([_i, _c_int_p, _i, _ll, _i], _sz),
     'cpab_backward': ([_i, _c_int_p, _i, _i, _vp, _i, _ll, _vp, _vp, _i, _vp, _i, _vp, _vp, _vp,
                        _vp, _sz, _vp, _vp], _i),
@@ -233,6 +236,32 @@ def integrate_exact(nc, points, A, ties=None, steps=None):
                                        n_theta, _ptr(out), _ptr(ties), _ptr(steps),
                                        _stream(points.device)))
     return out
+
+
+def backward_exact(nc, out, A, basis, grad_out, want_dpoints=False, ties=None, workspace=None):
+    """Gradient of integrate_exact: dtheta [n_theta, d] and dL/dpoints per theta
+    [n_theta, ndim, nP] (or None) from out = integrate_exact(...) [n_theta, ndim,
+    nP] and dL/d(out)."""
+    _require(out, 'out')
+    _require(A, 'A')
+    _require(basis, 'basis')
+    _require(grad_out, 'grad_out')
+    ndim = len(nc)
+    n_theta, nP = out.shape[0], out.shape[-1]
+    d = basis.shape[1]
+    dev = out.device
+    dtheta = torch.empty((n_theta, d), device=dev, dtype=torch.float32)
+    dpoints = torch.empty_like(out) if want_dpoints else None
+    lib = load()
+    need = lib.cpab_backward_exact_workspace(ndim, _ints(nc), nP, n_theta)
+    if need == 0 and nP > 0 and n_theta > 0:
+        _check(3)
+    if workspace is None or workspace.numel() < need:
+        workspace = torch.empty(max(need, 1), device=dev, dtype=torch.uint8)
+    _check(lib.cpab_backward_exact(ndim, _ints(nc), _ptr(out), nP, _ptr(A), n_theta,
+                                   _ptr(basis), d, _ptr(grad_out), _ptr(dtheta), _ptr(dpoints),
+                                   _ptr(workspace), workspace.numel(), _ptr(ties), _stream(dev)))
+    return dtheta, dpoints
 
 
 def integrate_trace(nc, nsteps, points, E):

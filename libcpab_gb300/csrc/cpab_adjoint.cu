@@ -272,6 +272,13 @@ cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *pa
         kern<<<n_theta, block, smem, s>>>(t.nC, st, partials, parts, A, basis, d, dtheta);     \
         return cudaGetLastError();                                                             \
     }
+    if (mode == kFinalizeDirect) {   // the partials are dL/dA (exact-flow adjoint)
+        switch (t.ndim) {
+            case 1: CPAB_FIN(1, 3)
+            case 2: CPAB_FIN(2, 3)
+            default: CPAB_FIN(3, 3)
+        }
+    }
     if (mode != 1) {   // modes 0 and 2: the midpoint sensitivity's cell map
         switch (t.ndim) {
             case 1: CPAB_FIN(1, 0)

@@ -553,9 +553,10 @@ __device__ __forceinline__ void adjoint_epilogue(const AdjSmem<N, CT> &sm, int n
 // recursion on Y/2^s, E/2^s followed by s squarings:
 //   R_{k-1} = I + (Y/k) R_k,  dR_{k-1} = (E/k) R_k + (Y/k) dR_k,
 //   then  L <- L R + R L,  R <- R R.
+// Rout receives R = expm(Y) (the overload without it drops R).
 template <int K>
 __device__ __forceinline__ void frechet_expm(const float (&Y0)[K][K], const float (&E0)[K][K],
-                                             float (&L)[K][K]) {
+                                             float (&L)[K][K], float (&Rout)[K][K]) {
     float norm = 0.f;
 #pragma unroll
     for (int j = 0; j < K; ++j) {
@@ -622,14 +623,25 @@ __device__ __forceinline__ void frechet_expm(const float (&Y0)[K][K], const floa
     for (int i = 0; i < K; ++i)
 #pragma unroll
         for (int j = 0; j < K; ++j) L[i][j] = D[i][j];
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+#pragma unroll
+        for (int j = 0; j < K; ++j) Rout[i][j] = R[i][j];
+}
+
+template <int K>
+__device__ __forceinline__ void frechet_expm(const float (&Y0)[K][K], const float (&E0)[K][K],
+                                             float (&L)[K][K]) {
+    float R[K][K];
+    frechet_expm<K>(Y0, E0, L, R);
 }
 
 // Per-theta tail of the finalize kernels, run by one block after the summed
 // cell statistics are in g (shared memory, nC * N*(N+1) floats; red is
 // blockDim.x floats of shared scratch): map them to
 // dL/dA (mode 0: G = h S (I + h/2 [A;0])^T + h^2/2 A_lin^T S; mode 1: adjoint
-// Frechet derivative of expm) and contract with the basis,
-// dtheta[k] = sum_i B[i, k] dA[i].
+// Frechet derivative of expm; mode 3, the exact-flow adjoint: already dL/dA)
+// and contract with the basis, dtheta[k] = sum_i B[i, k] dA[i].
 template <int N, int MODE>
 __device__ __forceinline__ void finish_theta(float *g, float *red, const float *__restrict__ A_th,
                                              int nC, const Steps &st,
@@ -637,7 +649,9 @@ __device__ __forceinline__ void finish_theta(float *g, float *red, const float *
                                              float *__restrict__ dth) {
     constexpr int P = N * (N + 1);
     const int tid = threadIdx.x, B = blockDim.x, G = nC * P;
-    if constexpr (MODE != 1) {
+    if constexpr (MODE == 3) {
+        // the exact-flow adjoint's partials are dL/dA already
+    } else if constexpr (MODE != 1) {
         // S_c = sum_n lambda_{n+1} [p_n;1]^T  ->
         // G_c = h S_c (I + h/2 [A_c;0])^T + h^2/2 A_lin^T S_c
         for (int c = tid; c < nC; c += B) {

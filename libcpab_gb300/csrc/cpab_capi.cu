@@ -193,6 +193,56 @@ int cpab_integrate_exact(int ndim, const int *nc, const float *points, int broad
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "exact-flow launch");
 }
 
+size_t cpab_backward_exact_workspace(int ndim, const int *nc, long long nP, int n_theta) {
+    g_err[0] = 0;
+    Tess t;
+    if (make_tess(ndim, nc, &t)) return 0;
+    if (nP <= 0 || n_theta <= 0) return 0;
+    AdjointPlan plan;
+    if (!plan_adjoint_exact(t, nP, n_theta, &plan)) {
+        fail(CPAB_ERR_UNSUPPORTED, "tessellation too large for the exact-flow adjoint");
+        return 0;
+    }
+    return plan.partial_floats * sizeof(float);
+}
+
+int cpab_backward_exact(int ndim, const int *nc, const float *out, long long nP, const float *A,
+                        int n_theta, const float *basis, int d, const float *grad_out,
+                        float *dtheta, float *dpoints, void *workspace, size_t workspace_bytes,
+                        unsigned long long *ties, void *stream) {
+    g_err[0] = 0;
+    Tess t;
+    int rc = make_tess(ndim, nc, &t);
+    if (rc) return rc;
+    if (nP < 0 || n_theta < 0 || d < 0) return fail(CPAB_ERR_ARGUMENT, "invalid sizes");
+    if ((rc = check_theta_count(n_theta))) return rc;
+    if (n_theta == 0 || (d == 0 && !dpoints)) return CPAB_OK;
+    if (!A || (d > 0 && (!dtheta || !basis)))
+        return fail(CPAB_ERR_ARGUMENT, "dtheta, basis or A is NULL");
+    cudaStream_t s = as_stream(stream);
+    if (nP == 0) {
+        if (d == 0) return CPAB_OK;
+        cudaError_t e = cudaMemsetAsync(dtheta, 0, (size_t)n_theta * d * sizeof(float), s);
+        return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "memset");
+    }
+    if (!out || !grad_out) return fail(CPAB_ERR_ARGUMENT, "out or grad_out is NULL");
+    AdjointPlan plan;
+    if (!plan_adjoint_exact(t, nP, n_theta, &plan))
+        return fail(CPAB_ERR_UNSUPPORTED, "tessellation too large for the exact-flow adjoint");
+    const size_t need = plan.partial_floats * sizeof(float);
+    if (!workspace || workspace_bytes < need)
+        return fail(CPAB_ERR_WORKSPACE, "workspace of %zu bytes needed (got %zu)", need,
+                    workspace ? workspace_bytes : (size_t)0);
+    float *partials = static_cast<float *>(workspace);
+    cudaError_t e = launch_adjoint_exact(t, plan, out, nP, A, n_theta, grad_out, dpoints,
+                                         partials, ties, device_error_word(), s);
+    if (e != cudaSuccess) return cuda_fail(e, "exact-flow adjoint launch");
+    if (d == 0) return CPAB_OK;
+    e = launch_finalize(t, 1, kFinalizeDirect, partials, plan.parts, A, basis, d, n_theta,
+                        dtheta, s);
+    return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "finalize launch");
+}
+
 int cpab_integrate_trace(int ndim, const int *nc, int nsteps, const float *points, int broadcast,
                          long long nP, const float *E, int n_theta, float *out, int *cells,
                          void *stream) {

@@ -87,6 +87,8 @@ cudaError_t launch_adjoint(const Tess &t, int nsteps, int mode, const AdjointPla
 // Sum the partials (fixed order), map cell gradients to dL/dA (mode 1: through
 // the adjoint Frechet derivative of expm), and contract with the basis:
 // dtheta[theta, k] = sum_i B[i, k] dA[i].
+// mode kFinalizeDirect: the partials are dL/dA (the exact-flow adjoint).
+constexpr int kFinalizeDirect = 3;
 cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *partials, int parts,
                             const float *A, const float *basis, int d, int n_theta,
                             float *dtheta, cudaStream_t s);
@@ -156,6 +158,15 @@ cudaError_t launch_integrate_exact(const Tess &t, const float *points, int broad
                                    long long nP, const float *A, int n_theta, float *out,
                                    unsigned long long *ties, unsigned *err,
                                    unsigned long long *steps, cudaStream_t s);
+
+// Reverse-mode derivative of the exact flow (cpab_exact.cu): from the forward
+// result out [n_theta, ndim, nP] and dL/d(out), per-CTA partial dL/dA for
+// launch_finalize(kFinalizeDirect) and dL/dpoints (may be NULL).
+bool plan_adjoint_exact(const Tess &t, long long nP, int n_theta, AdjointPlan *plan);
+cudaError_t launch_adjoint_exact(const Tess &t, const AdjointPlan &plan, const float *out,
+                                 long long nP, const float *A, int n_theta, const float *gout,
+                                 float *dpoints, float *partials, unsigned long long *ties,
+                                 unsigned *err, cudaStream_t s);
 
 // Ragged batched 1D series (cpab_ragged.cu).  Series s has the points
 // torch.linspace(0, 1, L_s) and the values values[off[s] .. off[s+1]).

@@ -553,3 +553,56 @@ def exact_flow_fp64(basis, theta, points, nc, rtol=1e-12, atol=1e-13):
                         atol=atol)
         out[k] = sol.y[:, -1].reshape(ndim, nP)
     return out
+
+
+def exact_flow_grad_fp64(basis, theta, points, nc, cot, rtol=1e-10, atol=1e-12):
+    """Gradient of the exact flow for time 1, in float64: (dtheta [n_theta, d],
+    dpoints [n_theta, ndim, nP]) of L = sum(cot * phi_1(points)).
+
+    Forward sensitivities, independent of the kernels' reverse sweep: the
+    state of a point is its position p, S = dp/dtheta [ndim, d] and
+    J = dp/dp0 [ndim, ndim], integrated together by DOP853:
+        dp/dt = A_c p~,   dS/dt = A_c,lin S + dv/dtheta,   dJ/dt = A_c,lin J,
+    with dv_i/dtheta_k = sum_j B[c, i, j, k] p~_j (A_c = B_c theta, the cell
+    of p by the C++ rules).  The field is continuous across faces, so the
+    sensitivities are continuous too and need no jump conditions.  Each point
+    is integrated on its own: the right-hand side is discontinuous where the
+    point crosses a face, and a joint system would take small steps at every
+    crossing of every point."""
+    from scipy.integrate import solve_ivp
+    nc = list(nc)
+    ndim = len(nc)
+    B = np.asarray(basis, dtype=np.float64)
+    th = np.asarray(theta, dtype=np.float64)
+    d = B.shape[1]
+    nC = B.shape[0] // (ndim * (ndim + 1))
+    Br = B.reshape(nC, ndim, ndim + 1, d)
+    pts = np.asarray(points, dtype=np.float64)
+    nP = pts.shape[-1]
+    cot = np.asarray(cot, dtype=np.float64)
+    dth = np.zeros((th.shape[0], d))
+    dpts = np.zeros((th.shape[0], ndim, nP))
+    n_s = ndim * d
+    for k in range(th.shape[0]):
+        A = (B @ th[k]).reshape(nC, ndim, ndim + 1)
+        p0s = pts[k] if pts.ndim == 3 else pts
+
+        def field(_t, y):
+            p = y[:ndim]
+            S = y[ndim:ndim + n_s].reshape(ndim, d)
+            J = y[ndim + n_s:].reshape(ndim, ndim)
+            c = int(numpy_findcellidx(ndim, p.reshape(ndim, 1).astype(np.float32), nc,
+                                      semantics='cpp')[0])
+            Ac = A[c]
+            ph = np.append(p, 1.0)
+            return np.concatenate([Ac @ ph, (Ac[:, :ndim] @ S + np.einsum('ijk,j->ik', Br[c], ph))
+                                   .reshape(-1), (Ac[:, :ndim] @ J).reshape(-1)])
+        for q in range(nP):
+            y0 = np.concatenate([p0s[:, q], np.zeros(n_s), np.eye(ndim).reshape(-1)])
+            sol = solve_ivp(field, (0.0, 1.0), y0, method='DOP853', rtol=rtol, atol=atol)
+            y = sol.y[:, -1]
+            S = y[ndim:ndim + n_s].reshape(ndim, d)
+            J = y[ndim + n_s:].reshape(ndim, ndim)
+            dth[k] += cot[k][:, q] @ S
+            dpts[k][:, q] = cot[k][:, q] @ J
+    return dth, dpts
