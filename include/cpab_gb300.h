@@ -374,7 +374,8 @@ CPAB_API int cpab_ragged1d_mse(int nc, int nsteps, int mode, const float *A, con
  * as cpab_ragged1d_mse) kernels on these inputs, keeps the fastest for later
  * calls with the same (device, kind, mode, nc, nsteps, S, total), and leaves
  * the outputs of the chosen shape in out (kind 0) or out/sse/dtheta/dvalues
- * (kind 1).  shape (may be NULL) receives {threads, points per lane};
+ * (kind 1).  force (may be NULL): {threads, points per lane} to keep without
+ * timing.  shape (may be NULL) receives {threads, points per lane};
  * best_ms (may be NULL) the fastest time.  Synchronises the stream; refuses
  * to run while the stream is being captured.
  */
@@ -383,7 +384,8 @@ CPAB_API int cpab_ragged1d_tune(int kind, int nc, int nsteps, int mode, const fl
                                 const float *basis, int d, const float *values,
                                 const float *target, float loss_scale, float *out, float *sse,
                                 float *dtheta, float *dvalues, void *workspace,
-                                size_t workspace_bytes, int *shape, float *best_ms, void *stream);
+                                size_t workspace_bytes, const int *force, int *shape,
+                                float *best_ms, void *stream);
 
 /*
  * Ragged point sets: S sets of ndim-dimensional points, each moved by its

@@ -68,7 +68,7 @@ _SIGS = {
     'cpab_ragged1d_mse': ([_i, _i, _i, _vp, _vp, _i, _vp, _ll, _vp, _i, _vp, _vp, ctypes.c_float,
                            _vp, _vp, _vp, _vp, _vp, _sz, _vp, _vp], _i),
     'cpab_ragged1d_tune': ([_i, _i, _i, _i, _vp, _vp, _i, _vp, _ll, _vp, _i, _vp, _vp,
-                            ctypes.c_float, _vp, _vp, _vp, _vp, _vp, _sz, _c_int_p,
+                            ctypes.c_float, _vp, _vp, _vp, _vp, _vp, _sz, _c_int_p, _c_int_p,
                             ctypes.POINTER(ctypes.c_float), _vp], _i),
     'cpab_ragged_points_workspace': ([_i, _c_int_p, _i], _sz),
     'cpab_ragged_points_forward': ([_i, _c_int_p, _i, _vp, _i, _vp, _ll, _vp, _vp, _vp, _sz, _vp,
@@ -534,14 +534,17 @@ def ragged_mse(nc, nsteps, mode, A, E, offsets, values, target, basis, loss_scal
 
 
 def ragged_tune(kind, nc, nsteps, mode, A, E, offsets, values, target, basis, loss_scale=None,
-                workspace=None):
-    """Autotune the ragged forward (kind 0) or adjoint (kind 1) launch shape on
-    these inputs.  Returns ((threads, points per lane), best ms, outputs)."""
+                workspace=None, force=None):
+    """Autotune (or, with force = (threads, points per lane), pin) the ragged
+    forward (kind 0) or adjoint (kind 1) launch shape on these inputs.
+    Returns ((threads, points per lane), best ms, outputs)."""
     args, res, dev = _mse_args(nc, nsteps, mode, A, E, offsets, values, target, basis,
                                loss_scale, True, True, workspace)
+    f = None if force is None else (ctypes.c_int * 2)(int(force[0]), int(force[1]))
     shape = (ctypes.c_int * 2)(0, 0)
     ms = ctypes.c_float(0.0)
-    _check(load().cpab_ragged1d_tune(int(kind), *args, shape, ctypes.byref(ms), _stream(dev)))
+    _check(load().cpab_ragged1d_tune(int(kind), *args, f, shape, ctypes.byref(ms),
+                                     _stream(dev)))
     return (shape[0], shape[1]), ms.value, res
 
 

@@ -865,7 +865,8 @@ int cpab_ragged1d_tune(int kind, int nc, int nsteps, int mode, const float *A, c
                        int S, const long long *offsets, long long total, const float *basis,
                        int d, const float *values, const float *target, float loss_scale,
                        float *out, float *sse, float *dtheta, float *dvalues, void *workspace,
-                       size_t workspace_bytes, int *shape, float *best_ms, void *stream) {
+                       size_t workspace_bytes, const int *force, int *shape, float *best_ms,
+                       void *stream) {
     g_err[0] = 0;
     Tess t;
     int rc = check_ragged(nc, nsteps, S, total, offsets, &t);
@@ -906,12 +907,28 @@ int cpab_ragged1d_tune(int kind, int nc, int nsteps, int mode, const float *A, c
     };
     const int blocks[3] = {64, 128, 256};
     const int ppts[3] = {1, 2, 4};
+    const int n_ppt = 3;
     float best = 3.0e38f;
     int bb = 0, bp = 0;
-    for (int bi = 0; bi < 3 && rc == CPAB_OK; ++bi) {
+    if (force) {   // one shape, validated, kept without timing
+        bool ok_b = false, ok_p = false;
+        for (int bi = 0; bi < 3; ++bi) ok_b |= force[0] == blocks[bi];
+        for (int pi = 0; pi < n_ppt; ++pi) ok_p |= force[1] == ppts[pi];
+        if (!ok_b || !ok_p ||
+            (kind == kRaggedAdjoint && !ragged_adjoint_smem_for(t, nsteps, mode, force[0]))) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return fail(CPAB_ERR_ARGUMENT, "launch shape {%d, %d} is not one of the candidates "
+                        "that fit", force[0], force[1]);
+        }
+        bb = force[0];
+        bp = force[1];
+        best = 0.f;
+    }
+    for (int bi = 0; bi < 3 && rc == CPAB_OK && !force; ++bi) {
         if (kind == kRaggedAdjoint && !ragged_adjoint_smem_for(t, nsteps, mode, blocks[bi]))
             continue;
-        for (int pi = 0; pi < 3 && rc == CPAB_OK; ++pi) {
+        for (int pi = 0; pi < n_ppt && rc == CPAB_OK; ++pi) {
             if ((rc = run(blocks[bi], ppts[pi]))) break;   // warm-up
             float ms = 3.0e38f;
             for (int rep = 0; rep < 3 && rc == CPAB_OK; ++rep) {

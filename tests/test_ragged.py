@@ -268,6 +268,34 @@ def test_ragged_autotune(cuda):
                        base['out'])
 
 
+def test_ragged_every_launch_shape(cuda):
+    """Every candidate launch shape of the ragged kernels pinned in turn (the
+    tuner's force argument): forward output bit-identical to the default
+    shape's; the adjoint's out bit-identical, the squared errors and dtheta
+    within 1e-5 (other block sizes and passes per tile change only the order
+    of the sums; d(values), a float-atomic scatter like the reference's, is
+    checked against its summation bound elsewhere)."""
+    P = _problem(cuda, 20, [int(x) for x in np.random.default_rng(2).integers(1, 2500, 48)])
+    N = P['N']
+    base = N.ragged_mse(P['nc'], NSTEPS, 0, P['A'], P['E'], P['off'], P['values'], P['target'],
+                        P['basis'], want_out=True)
+    for kind in (0, 1):
+        for b in (64, 128, 256):
+            for ppt in (1, 2, 4):
+                shape, ms, res = N.ragged_tune(kind, P['nc'], NSTEPS, 0, P['A'], P['E'],
+                                               P['off'], P['values'], P['target'], P['basis'],
+                                               force=(b, ppt))
+                assert tuple(shape) == (b, ppt) and ms == 0.0
+                assert torch.equal(res['out'], base['out']), (kind, b, ppt)
+                if kind == 1:
+                    assert _rel(res['sse'], base['sse']) <= 1e-5, (b, ppt)
+                    assert _rel(res['dtheta'], base['dtheta']) <= 1e-5, (b, ppt)
+    with pytest.raises(N.CpabError):
+        N.ragged_tune(1, P['nc'], NSTEPS, 0, P['A'], P['E'], P['off'], P['values'],
+                      P['target'], P['basis'], force=(96, 1))
+    assert N.device_status() == 0
+
+
 def test_ragged_empty_and_invalid_series(cuda):
     from libcpab_gb300 import _native as N
     P = _problem(cuda, 10, [0, 0, 0])
