@@ -65,7 +65,7 @@ def parse():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--leg', default='all',
                     choices=['all', 'ragged', 'volume', 'interp', 'aligner', 'exact', 'points',
-                             'mixed', 'plain'],
+                             'mixed', 'plain', 'cfg1', 'cfg5'],
                     help='run only one of the side workloads and print its result (for '
                          'profiling runs)')
     ap.add_argument('--no-tune', action='store_true',
@@ -343,6 +343,8 @@ def run_gb300(args):
     interp = run_interp_sweep(device, args.steps, flush) if extra else None
     aligner = run_aligner(device) if extra else None
     exact = run_exact_flow(device, args.steps, flush) if extra else None
+    cfg1 = run_cfg1(device, args.steps, flush) if extra else None
+    cfg5 = run_cfg5(device, args.steps, flush) if extra else None
     points = run_ragged_points(device, args.steps, flush, tune=not args.no_tune) if extra else None
     mixed = run_mixed_images(device, args.steps, flush) if extra else None
     # results of the timed inputs on the first images, for the check against
@@ -482,6 +484,8 @@ def run_gb300(args):
             'interpolate_2d': interp,
             'aligner': aligner,
             'exact_flow': exact,
+            'cfg1_transform_grid_1d': cfg1,
+            'cfg5_precision_stress_2d': cfg5,
             'ragged_points_2d': points,
             'mixed_size_images_2d': mixed,
             'clocks': clk, 'device_status': status,
@@ -972,6 +976,147 @@ def run_exact_flow(device, steps, flush):
             'max_abs_diff_exact_vs_fixed_step': float((ex - fs).abs().max())}
 
 
+def trajectory_errors(B, theta, pts, nc, out, cells):
+    """GPU trajectories [n, ndim, nP] (with their cells [n, nP, nsteps])
+    against the FP64 oracle of the same scheme (C++ cell rules): max and p99
+    error of the trajectories with the oracle's cells (scaled by max(1, |p|)),
+    and the others (boundary ties) with the margin at their first divergence."""
+    from oracle.oracle import numpy_transform_grid
+    ref, cells64, marg = numpy_transform_grid(B, theta, pts, nc, NSTEPS, return_cells=True,
+                                              return_margin='steps', semantics='cpp')
+    diff = cells != cells64
+    tie = diff.any(axis=2)
+    err = np.abs(out - ref).max(axis=1) / np.maximum(1.0, np.abs(ref).max(axis=1))
+    first = diff.argmax(axis=2)
+    ti, pi = np.nonzero(tie)
+    fm = marg[ti, pi, first[ti, pi]] if ti.size else np.zeros(0)
+    clean = err[~tie]
+    return {'trajectories': int(err.size),
+            'clean_max_err': float(clean.max()) if clean.size else 0.0,
+            'clean_p99_err': float(np.quantile(clean, 0.99)) if clean.size else 0.0,
+            'tie_trajectories': int(tie.sum()),
+            'tie_first_margin_max': float(fm.max()) if fm.size else 0.0}
+
+
+def run_cfg1(device, steps, flush):
+    """The reference's CPU-runnable configuration: tess [50] zero_boundary,
+    16 theta ~ N(0, I), transform_grid of the 1,000-point meshgrid.  Forward
+    (cell tables + integration) and forward + dtheta backward through the
+    public API on the GPU; beside them the reference's own compiled C++ op
+    (pytorch-CPU path, its fp32 step maps) and the FP64 restatement of its
+    numpy backend on one host core each, and the GPU's error against FP64."""
+    from libcpab_gb300 import Cpab, _native as N
+    from libcpab_gb300.functions import basis_on
+    from oracle.oracle import RefLib, numpy_transform_grid
+    nc = [50]
+    T = Cpab(nc, backend='pytorch', device='gpu', zero_boundary=True)
+    theta = torch.randn(16, T.get_theta_dim(), generator=torch.Generator().manual_seed(0))
+    th = theta.to(device)
+    grid = T.uniform_meshgrid([1000])
+    fwd = lambda: T.transform_grid(grid, th)
+
+    def fwd_bwd():
+        t = th.detach().requires_grad_(True)
+        T.transform_grid(grid, t).sum().backward()
+    for _ in range(5):
+        fwd()
+        fwd_bwd()
+    n = max(steps, 20)
+    tf, tb = time_events(fwd, n, flush), time_events(fwd_bwd, n, flush)
+    basis = basis_on(T.params, device)
+    _, Tt, E = N.cell_tables(nc, NSTEPS, th, basis, want_T=True)
+    out, cells = N.integrate_trace(nc, NSTEPS, grid, E)
+    B = T.params.basis
+    pts = grid.cpu().numpy()
+    errs = trajectory_errors(B, theta.numpy(), pts, nc, out.cpu().numpy(), cells.cpu().numpy())
+    pts_n = 16 * 1000
+    res = {'workload': 'transform_grid, tess [50] zero_boundary, 16 theta ~ N(0,I), 1,000-point '
+                       'meshgrid', 'forward_ms': sum(tf) / len(tf),
+           'forward_points_per_s': pts_n / (sum(tf) / len(tf) / 1e3),
+           'fwd_bwd_ms': sum(tb) / len(tb),
+           'fwd_bwd_points_per_s': pts_n / (sum(tb) / len(tb) / 1e3),
+           'error_vs_fp64': errs}
+    # the reference's CPU paths on the same inputs (one core each)
+    try:
+        ref = RefLib()
+        trels = Tt.cpu().numpy()
+        ref.forward(nc, NSTEPS, pts, trels)
+        t0 = time.perf_counter()
+        reps = 20
+        for _ in range(reps):
+            ref.forward(nc, NSTEPS, pts, trels)
+        ms = (time.perf_counter() - t0) / reps * 1e3
+        res['reference_cpp_cpu_forward'] = {'ms': ms, 'points_per_s': pts_n / (ms / 1e3),
+                                            'cores': 1}
+    except (OSError, FileNotFoundError) as e:
+        res['reference_cpp_cpu_forward'] = {'unavailable': str(e)[:200]}
+    t0 = time.perf_counter()
+    numpy_transform_grid(B, theta.numpy(), pts, nc, NSTEPS)
+    ms = (time.perf_counter() - t0) * 1e3
+    res['reference_numpy_fp64_forward'] = {'ms': ms, 'points_per_s': pts_n / (ms / 1e3),
+                                           'cores': 1,
+                                           'path': 'FP64 restatement of the numpy backend'}
+    return res
+
+
+def run_cfg5(device, steps, flush):
+    """The precision-stress configuration: tess [8,8] without zero boundary
+    (d = 234), 256 theta ~ N(0, 9 I) and 256 theta ~ 1e-6 N(0, I), the 512 x
+    512 grid per theta (134 M trajectories): transform_grid forward and its
+    dtheta backward (reference gradient) on the GPU, the FP64-path lookups
+    over the whole run, and the error against the FP64 oracle on a sample
+    (8 theta of each group x 1,024 grid points)."""
+    from libcpab_gb300 import Cpab, _native as N
+    from libcpab_gb300.functions import basis_on
+    nc = [8, 8]
+    T = Cpab(nc, backend='pytorch', device='gpu', zero_boundary=False)
+    d = T.get_theta_dim()
+    g = torch.Generator().manual_seed(0)
+    theta = torch.cat([3.0 * torch.randn(256, d, generator=g),
+                       1e-6 * torch.randn(256, d, generator=g)])
+    th = theta.to(device)
+    lin = torch.linspace(0, 1, 512)
+    gx, gy = torch.meshgrid(lin, lin, indexing='xy')
+    grid = torch.stack([gx.reshape(-1), gy.reshape(-1)]).contiguous()
+    P = grid.to(device)
+    basis = basis_on(T.params, device)
+    A, _, E = N.cell_tables(nc, NSTEPS, th, basis)
+    ties = torch.zeros(1, dtype=torch.int64, device=device)
+    out = N.integrate(nc, NSTEPS, P, E, ties=ties)
+    fp64_lookups = int(ties.item())
+    cot = torch.randn(out.shape, generator=torch.Generator().manual_seed(1)).to(device)
+    ws = torch.empty(N.load().cpab_backward_workspace(2, N._ints(nc), NSTEPS, P.shape[1], 512),
+                     dtype=torch.uint8, device=device)
+    fwd = lambda: N.integrate(nc, NSTEPS, P, E)
+    bwd = lambda: N.backward(nc, NSTEPS, 0, P, A, E, basis, cot, workspace=ws)
+    for _ in range(2):
+        fwd()
+        bwd()
+    n = max(2, steps // 3)
+    tf, tb = time_events(fwd, n, flush), time_events(bwd, n, flush)
+    pts_n = 512 * 512 * 512
+    # sample: 8 theta of each group x 1,024 grid points
+    rows = torch.cat([torch.arange(0, 8), torch.arange(256, 264)])
+    cols = torch.tensor(np.sort(np.random.default_rng(2).choice(512 * 512, 1024, replace=False)))
+    Ps = P[:, cols.to(device)].contiguous()
+    errs = {}
+    for name, r in (('large_velocities', rows[:8]), ('near_identity', rows[8:])):
+        o, c = N.integrate_trace(nc, NSTEPS, Ps, E[r.to(device)].contiguous())
+        errs[name] = trajectory_errors(T.params.basis, theta[r].numpy(), Ps.cpu().numpy(), nc,
+                                       o.cpu().numpy(), c.cpu().numpy())
+    del out, cot, ws
+    torch.cuda.empty_cache()
+    return {'workload': 'transform_grid, tess [8,8] free, 256 theta ~ N(0,9I) + 256 theta ~ '
+                        '1e-6 N(0,I), 512^2 grid per theta (134 M trajectories); backward: '
+                        'dtheta (reference gradient, d = 234) for a N(0,1) cotangent',
+            'forward_ms': sum(tf) / len(tf),
+            'forward_points_per_s': pts_n / (sum(tf) / len(tf) / 1e3),
+            'backward_ms': sum(tb) / len(tb),
+            'fwd_bwd_points_per_s': pts_n / ((sum(tf) / len(tf) + sum(tb) / len(tb)) / 1e3),
+            'fp64_path_lookups': fp64_lookups, 'lookups': pts_n * NSTEPS,
+            'error_vs_fp64': errs}
+
+
 CPU_SAMPLE_IMAGES, CPU_STEPS = 4, 3
 
 
@@ -1165,6 +1310,8 @@ def main():
               'interp': lambda: run_interp_sweep(device, args.steps, flush),
               'aligner': lambda: run_aligner(device),
               'exact': lambda: run_exact_flow(device, args.steps, flush),
+              'cfg1': lambda: run_cfg1(device, args.steps, flush),
+              'cfg5': lambda: run_cfg5(device, args.steps, flush),
               'points': lambda: run_ragged_points(device, args.steps, flush,
                                                   tune=not args.no_tune),
               'mixed': lambda: run_mixed_images(device, args.steps, flush),
