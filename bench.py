@@ -362,6 +362,13 @@ def run_gb300(args):
     plain = None
     if rank == 0 and not args.no_plain:
         plain = run_plain_gpu_reference(device, theta, data, target, flush)
+        if extra and 'unavailable' not in plain:
+            tg = run_plain_transform_grid(device, flush)
+            if cfg1 and 'cfg1_forward_ms' in tg:
+                tg['cfg1_forward_speedup'] = tg['cfg1_forward_ms'] / cfg1['forward_ms']
+            if cfg5 and 'cfg5_forward_ms' in tg:
+                tg['cfg5_forward_speedup'] = tg['cfg5_forward_ms'] / cfg5['forward_ms']
+            plain['transform_grid_forward'] = tg
         if '_result' in plain:
             p_loss, p_dth, p_dd, p_grid, p_out = plain.pop('_result')
             # this library's fused backward fed the reference's own warped grid
@@ -795,6 +802,44 @@ def run_plain_gpu_reference(device, theta, data, target, flush, steps=PLAIN_STEP
                                         '(873 MB) fits',
             'basis_max_abs_diff_vs_this_library': basis_diff,
             '_result': (loss, dth, dd, ref_grid, ref_out)}
+
+
+def run_plain_transform_grid(device, flush, steps=3):
+    """The reference's own GPU transform_grid (forward: its basis upload, Pade
+    expm and cpab_gpu forward kernel) on the cfg1 and cfg5 inputs of
+    run_cfg1 / run_cfg5 (same seeds), for the forward ratio beside the
+    headline's.  The reference builds its basis on this machine (override)."""
+    try:
+        from baseline import plain_gpu
+        ref = plain_gpu.load()
+        res = {}
+        # cfg1: tess [50] zero boundary, 16 theta ~ N(0, I), 1,000-point meshgrid
+        T1 = ref.Cpab([50], backend='pytorch', device='gpu', zero_boundary=True, override=True)
+        th1 = torch.randn(16, T1.get_theta_dim(),
+                          generator=torch.Generator().manual_seed(0)).to(device)
+        g1 = T1.uniform_meshgrid([1000])
+        for _ in range(3):
+            T1.transform_grid(g1, th1)
+        t = time_events(lambda: T1.transform_grid(g1, th1), max(steps, 10), flush)
+        res['cfg1_forward_ms'] = statistics.median(t)
+        # cfg5: tess [8,8] free, 256 theta ~ N(0, 9 I) + 256 ~ 1e-6 N(0, I), 512^2 grid
+        T5 = ref.Cpab([8, 8], backend='pytorch', device='gpu', zero_boundary=False,
+                      override=True)
+        d = T5.get_theta_dim()
+        g = torch.Generator().manual_seed(0)
+        th5 = torch.cat([3.0 * torch.randn(256, d, generator=g),
+                         1e-6 * torch.randn(256, d, generator=g)]).to(device)
+        lin = torch.linspace(0, 1, 512)
+        gx, gy = torch.meshgrid(lin, lin, indexing='xy')
+        g5 = torch.stack([gx.reshape(-1), gy.reshape(-1)]).contiguous().to(device)
+        T5.transform_grid(g5, th5[:16])
+        t = time_events(lambda: T5.transform_grid(g5, th5), max(1, steps), flush)
+        res['cfg5_forward_ms'] = statistics.median(t)
+        res['path'] = ("reference libcpab, unmodified: Cpab.transform_grid (backend='pytorch', "
+                       "device='gpu'), forward only, all theta in one call")
+        return res
+    except Exception as e:    # the comparator is optional: report, do not fail the bench
+        return {'unavailable': '%s: %s' % (type(e).__name__, str(e)[:300])}
 
 
 def run_plain_leg(device, steps, flush):
