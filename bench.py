@@ -399,7 +399,8 @@ def run_gb300(args):
                 (p_dth - e_dth).abs().max() / e_dth.abs().max())
             plain['ddata_rel_diff_vs_this_library'] = float(
                 (p_dd - e_dd).abs().max() / e_dd.abs().max())
-            plain['loss_rel_diff_vs_this_library'] = float(abs(p_loss - e_loss) / abs(e_loss))
+            e_l = e_loss.detach()
+            plain['loss_rel_diff_vs_this_library'] = float(abs(p_loss - e_l) / abs(e_l))
             del p_loss, p_dth, p_dd, p_grid, p_out
         torch.cuda.empty_cache()
     clk = clocks.stop() if clocks else None
