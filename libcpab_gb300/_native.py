@@ -151,7 +151,16 @@ def _ptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
+# The current stream's cudaStream_t: torch's raw-handle query where present
+# (torch.cuda.current_stream(device) normalises the device and builds a Stream
+# object on every call, a measurable share of an eager step's host time).
+_raw_stream = getattr(torch._C, '_cuda_getCurrentRawStream', None)
+
+
 def _stream(device) -> ctypes.c_void_p:
+    if _raw_stream is not None and isinstance(device, torch.device) and device.type == 'cuda':
+        idx = device.index if device.index is not None else torch.cuda.current_device()
+        return ctypes.c_void_p(_raw_stream(idx))
     return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
 
 

@@ -70,33 +70,40 @@ class HostUpload:
         n = host.shape[0] if host.dim() > 0 else 1
         self.bounds = chunk_bounds(n, chunks) if host.dim() > 0 else [(0, 1)]
         self.events = []
+        self.started = False
         with torch.cuda.stream(self._cs):
             # allocated on the copy stream: the allocator hands it a block
             # whose earlier users are ordered before the copy, so the copy
             # need not wait for the current stream's queued kernels
             self.tensor = torch.empty(host.shape, dtype=dtype, device=device)
+            if start:   # in the same stream context (one switch per upload)
+                self._enqueue()
         # consumers run on the current stream: the block is reused only after
         # their queued work is done
         self.tensor.record_stream(cur)
-        self.started = False
-        if start:
-            self.start()
+
+    def _enqueue(self):
+        # the copies and their events, on the copy stream (the current one)
+        self.started = True
+        host, cs = self.host, self._cs
+        if len(self.bounds) == 1:
+            self.tensor.copy_(host, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(cs)
+            self.events.append(ev)
+            return
+        for a, b in self.bounds:
+            self.tensor[a:b].copy_(host[a:b], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(cs)
+            self.events.append(ev)
 
     def start(self):
         """Enqueue the copies (once)."""
         if self.started:
             return
-        self.started = True
-        host, cs = self.host, self._cs
-        with torch.cuda.stream(cs):
-            for a, b in self.bounds:
-                if host.dim() > 0:
-                    self.tensor[a:b].copy_(host[a:b], non_blocking=True)
-                else:
-                    self.tensor.copy_(host, non_blocking=True)
-                ev = torch.cuda.Event()
-                ev.record(cs)
-                self.events.append(ev)
+        with torch.cuda.stream(self._cs):
+            self._enqueue()
 
     def wait(self, k: int | None = None) -> torch.Tensor:
         self.start()
