@@ -332,7 +332,8 @@ int cpab_interpolate(int ndim, const float *data, int nb, int C, const int *size
     if (nb < 0 || C < 1) return fail(CPAB_ERR_ARGUMENT, "invalid nb or C");
     if (nb == 0) return CPAB_OK;
     if (!data || !grid || !out) return fail(CPAB_ERR_ARGUMENT, "data, grid or out is NULL");
-    cudaError_t e = launch_interpolate(ndim, data, nb, C, size, grid, outsize, out, as_stream(stream));
+    cudaError_t e = launch_interpolate(ndim, data, nb, C, size, grid, outsize, out,
+                                       device_error_word(), as_stream(stream));
     return e == cudaSuccess ? CPAB_OK : cuda_fail(e, "interpolate launch");
 }
 

@@ -21,6 +21,9 @@
 // Backward: d(data) is a scatter-add (float atomics into a zeroed buffer, like
 // the reference's autograd index_put accumulation); d(grid) follows the
 // gradient of the lerp weights, as autograd does through xd, yd, zd.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "cpab_interp.cuh"
 
 namespace cpab {
@@ -233,6 +236,129 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// 3D forward with the grid tile staged by the tensor memory accelerator.
+// One cp.async.bulk.tensor per image copies the tile's (32 x, 1 y, 32 z, 3
+// components) box of the grid into shared memory with the 128-byte swizzle
+// (the 128-byte row of x values of row R = 32 j + z_local has its 16-byte
+// chunks permuted by chunk ^ (R & 7)), double-buffered on two mbarriers, so
+// the staging costs no per-point instructions; points outside the image read
+// the zero fill.  Lane z_local then reads the four x values of its chunk
+// (x_local = 4 warp + u) with one 16-byte load per component, conflict-free
+// under the swizzle, and samples TP points at a time with all their corner
+// loads issued before the first lerp.  Corners are addressed from one base
+// pointer per point (CornerStep).  The output is stored directly: the lanes
+// of a warp write 32 consecutive z.  On 8 x 128^3 volumes this takes 0.095 ms
+// against 0.125 ms for k_interpolate_tiled<3, 1>: 110 instead of 183
+// instructions per point, identical results.  Four blocks per SM keep most
+// of L1 for the gathers (77 % sector hits; at six or eight blocks the shared
+// memory carve-out leaves too little L1 and the kernel slows down).
+constexpr int kTmaBox = 3 * kTile * kTile;   // floats per staged grid tile
+constexpr int kTmaSmem = 1024 + 2 * kTmaBox * 4 + 2 * 8;
+
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1,
+                                            int c2, int c3, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+        "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Points whose corner loads are issued together, and blocks per SM: the
+// gathered values of one group stay within 64 registers per thread for one
+// or two channels; three channels take one point at a time and up to 80
+// registers (four would spill: they use k_interpolate_tiled<3, 4>).
+template <int CC>
+__host__ __device__ constexpr int tma3_points_per_group() { return CC == 1 ? 4 : 1; }
+template <int CC>
+__host__ __device__ constexpr int tma3_blocks_per_sm() { return CC <= 2 ? 4 : 3; }
+
+template <int CC, bool FB>
+__global__ void __launch_bounds__(256, tma3_blocks_per_sm<CC>())
+    k_interpolate_tma3(const __grid_constant__ CUtensorMap gmap, Geo g, TileGeo tg,
+                       const float *__restrict__ data, float *__restrict__ out, int nb,
+                       unsigned *err) {
+    constexpr int N = 3, TP = tma3_points_per_group<CC>();
+    extern __shared__ unsigned char smem_raw[];
+    // the swizzle pattern follows address bits 7-9: 1024-byte aligned buffers
+    float *gbuf = reinterpret_cast<float *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bar = reinterpret_cast<uint64_t *>(gbuf + 2 * kTmaBox);
+    int a0, z0, mid;
+    tile_coords<N>(g, tg, blockIdx.x, a0, z0, mid);
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int A = g.outsize[0], Z = g.outsize[N - 1];
+    const bool leader = threadIdx.x == 0;
+    if (leader) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+    }
+    __syncthreads();
+    int b = blockIdx.y;
+    if (leader && b < nb) {
+        mbar_arrive_expect_tx(&bar[0], kTmaBox * 4);
+        tma_load_4d(gbuf, &gmap, a0, mid, z0, 3 * b, &bar[0]);
+    }
+    const int chunk = ((ty ^ (tx & 7)) << 4);   // byte offset of this lane's x chunk in its row
+    for (int k = 0; b < nb; b += gridDim.y, ++k) {
+        const int hb = k & 1;
+        const unsigned parity = (k >> 1) & 1;
+        const bool got = mbar_wait_bounded(&bar[hb], parity);
+        // every thread is done with the other buffer (image k - 1) past this barrier
+        if (__syncthreads_or(!got)) {
+            if (leader) raise_error(err, kErrTmaTimeout);
+            mbar_wait_bounded(&bar[hb], parity);   // a second bounded wait for the copy in flight
+            break;
+        }
+        if (leader && b + (int)gridDim.y < nb) {
+            mbar_arrive_expect_tx(&bar[hb ^ 1], kTmaBox * 4);
+            tma_load_4d(gbuf + (hb ^ 1) * kTmaBox, &gmap, a0, mid, z0, 3 * (b + gridDim.y),
+                        &bar[hb ^ 1]);
+        }
+        const unsigned char *gt = reinterpret_cast<const unsigned char *>(gbuf + hb * kTmaBox);
+        float pp[4][N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            const float4 q = *reinterpret_cast<const float4 *>(gt + (kTile * j + tx) * 128 + chunk);
+            pp[0][j] = q.x;
+            pp[1][j] = q.y;
+            pp[2][j] = q.z;
+            pp[3][j] = q.w;
+        }
+        const float *Db = data + (long long)b * CC * g.nD;
+        float *Ob = out + (long long)b * CC * g.nP;
+        const int z = z0 + tx;
+#pragma unroll
+        for (int u0 = 0; u0 < 4; u0 += TP) {
+            float v[TP][CC][1 << N];
+            float f[TP][N];
+#pragma unroll
+            for (int w = 0; w < TP; ++w) {
+                const CornerStep<N> cr = corner_steps<N, FB>(pp[u0 + w], g);
+#pragma unroll
+                for (int c = 0; c < CC; ++c) {
+                    const float *P = Db + (long long)c * g.nD + cr.base;
+#pragma unroll
+                    for (int m = 0; m < (1 << N); ++m) v[w][c][m] = __ldg(P + cr.delta(m));
+                }
+#pragma unroll
+                for (int j = 0; j < N; ++j) f[w][j] = cr.f[j];
+            }
+#pragma unroll
+            for (int w = 0; w < TP; ++w) {
+                const int a = a0 + 4 * ty + u0 + w;
+                if (a < A && z < Z) {
+                    const int o = out_index<N>(g, a, mid, z);
+#pragma unroll
+                    for (int c = 0; c < CC; ++c)
+                        Ob[(long long)c * g.nP + o] = lerp_values<N>(v[w][c], f[w]);
+                }
+            }
+        }
+    }
+}
+
 template <int N>
 __global__ void __launch_bounds__(256)
     k_interpolate_backward_tiled(Geo g, TileGeo tg, const float *__restrict__ data, int C,
@@ -296,9 +422,55 @@ static TileGeo make_tiles(int ndim, const Geo &g, unsigned *blocks) {
     return tg;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library); null where the driver does not provide it.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }();
+    return fn;
+}
+
+// The grid [nb, 3, D_out, H_out, W_out] (x fastest) as a 4D tensor map with
+// the (32, 1, 32, 3) box of k_interpolate_tma3.  False where the tensor
+// memory accelerator cannot address it: a grid not 16-byte aligned or a row
+// stride (W_out floats) not a multiple of 16 bytes.
+static bool encode_grid_map_3d(CUtensorMap *map, const float *grid, const int *outsize, int nb) {
+    const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || (reinterpret_cast<uintptr_t>(grid) & 15u) || (outsize[0] & 3)) return false;
+    const cuuint64_t W = outsize[0], H = outsize[1], D = outsize[2];
+    const cuuint64_t dims[4] = {W, H, D, (cuuint64_t)3 * nb};
+    const cuuint64_t strides[3] = {W * 4, W * H * 4, W * H * D * 4};
+    const cuuint32_t box[4] = {(cuuint32_t)kTile, 1, (cuuint32_t)kTile, 3};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float *>(grid), dims, strides,
+               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int CC>
+static cudaError_t launch_tma3(const CUtensorMap &map, const Geo &g, const TileGeo &tg,
+                               dim3 tgrid, const float *data, float *out, int nb, unsigned *err,
+                               cudaStream_t s) {
+    if (g.nD < (1 << 23))
+        k_interpolate_tma3<CC, true><<<tgrid, 256, kTmaSmem, s>>>(map, g, tg, data, out, nb, err);
+    else
+        k_interpolate_tma3<CC, false><<<tgrid, 256, kTmaSmem, s>>>(map, g, tg, data, out, nb, err);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_interpolate(int ndim, const float *data, int nb, int C, const int *size,
                                const float *grid, const int *outsize, float *out,
-                               cudaStream_t s) {
+                               unsigned *err, cudaStream_t s) {
     const Geo g = make_geo(ndim, size, outsize);
     if ((long long)nb * g.nP == 0) return cudaSuccess;
     const int block = 256;
@@ -312,6 +484,14 @@ cudaError_t launch_interpolate(int ndim, const float *data, int nb, int C, const
     const TileGeo tg = make_tiles(ndim, g, &blocks);
     const int ipb = ndim == 3 ? images_per_block<3>() : images_per_block<2>();
     const dim3 tgrid(blocks, (gridn.y + ipb - 1) / ipb);
+    CUtensorMap map;
+    if (ndim == 3 && C <= 3 && encode_grid_map_3d(&map, grid, outsize, nb)) {
+        switch (C) {
+            case 1: return launch_tma3<1>(map, g, tg, tgrid, data, out, nb, err, s);
+            case 2: return launch_tma3<2>(map, g, tg, tgrid, data, out, nb, err, s);
+            default: return launch_tma3<3>(map, g, tg, tgrid, data, out, nb, err, s);
+        }
+    }
 #define CPAB_IT(NN, CC) k_interpolate_tiled<NN, CC><<<tgrid, block, 0, s>>>(g, tg, data, C, grid, out, nb)
     if (ndim == 2) {
         switch (C) {

@@ -81,6 +81,61 @@ __device__ __forceinline__ float lerp_corners(const float *D, const Corner<N> &c
     return lerp_values<N>(v, cr.f);
 }
 
+// The same corners as one base offset plus one step per axis: corner m is at
+// base + the steps of the axes whose bit is set in m.  A gather then forms one
+// 64-bit address per point (P = D + base) and reaches the other corners by
+// 32-bit steps from it.  The step is the axis stride when x1 = x0 + 1 (floor
+// in [0, size - 2]) and 0 where both clamp to the same edge; floorf agrees with
+// corner_indices' float floor on every input (NaN included: the clamps map it
+// to 0).  FB: the base is accumulated in float, exact while the image has
+// fewer than 2^23 elements (every partial sum is an integer below 2^23).
+template <int N>
+struct CornerStep {
+    int base;
+    int step[N];
+    float f[N];
+    __device__ __forceinline__ int delta(int m) const {
+        int o = 0;
+#pragma unroll
+        for (int j = 0; j < N; ++j)
+            if ((m >> j) & 1) o += step[j];
+        return o;
+    }
+};
+
+template <int N, bool FB>
+__device__ __forceinline__ CornerStep<N> corner_steps(const float (&p)[N], const Geo &g) {
+    CornerStep<N> cr;
+    float a[N];
+    bool up[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        const float x = __fmul_rn(p[j], g.sizem1[j]);
+        const float fl = floorf(x);
+        a[j] = fminf(fmaxf(fl, 0.f), g.sizem1[j]);
+        cr.f[j] = __fsub_rn(x, a[j]);
+        up[j] = fl >= 0.f && fl < g.sizem1[j];
+    }
+    int st[N];   // element strides, last axis fastest
+    st[N - 1] = 1;
+#pragma unroll
+    for (int j = N - 2; j >= 0; --j) st[j] = st[j + 1] * g.size[j + 1];
+    if constexpr (FB) {
+        float bf = a[N - 1];
+#pragma unroll
+        for (int j = N - 2; j >= 0; --j) bf = __fmaf_rn(a[j], (float)st[j], bf);
+        cr.base = float_bits(__fadd_rn(bf, 8388608.f)) - 0x4B000000;   // + 2^23: integer bits
+    } else {
+        int o = 0;
+#pragma unroll
+        for (int j = 0; j < N; ++j) o += small_float_to_int(a[j]) * st[j];
+        cr.base = o;
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) cr.step[j] = up[j] ? st[j] : 0;
+    return cr;
+}
+
 // Offsets in corner order for lerp_corners: pass j pairs entries (2m, 2m+1),
 // so corner index bits must be ordered with axis 0 as the lowest bit after
 // each pass.  corners() builds index m with bit j = axis j; pass 0 pairs m

@@ -94,9 +94,10 @@ cudaError_t launch_finalize(const Tess &t, int nsteps, int mode, const float *pa
                             float *dtheta, cudaStream_t s);
 
 // Linear / bilinear / trilinear sampling (libcpab/pytorch/interpolation.py).
+// err: device error word (a timed-out grid-tile copy of the 3D kernel).
 cudaError_t launch_interpolate(int ndim, const float *data, int nb, int C, const int *size,
                                const float *grid, const int *outsize, float *out,
-                               cudaStream_t s);
+                               unsigned *err, cudaStream_t s);
 cudaError_t launch_interpolate_backward(int ndim, const float *data, int nb, int C,
                                         const int *size, const float *grid, const int *outsize,
                                         const float *gout, float *ddata, float *dgrid,
