@@ -236,25 +236,37 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-// 3D forward with the grid tile staged by the tensor memory accelerator.
-// One cp.async.bulk.tensor per image copies the tile's (32 x, 1 y, 32 z, 3
-// components) box of the grid into shared memory with the 128-byte swizzle
-// (the 128-byte row of x values of row R = 32 j + z_local has its 16-byte
-// chunks permuted by chunk ^ (R & 7)), double-buffered on two mbarriers, so
-// the staging costs no per-point instructions; points outside the image read
-// the zero fill.  Lane z_local then reads the four x values of its chunk
-// (x_local = 4 warp + u) with one 16-byte load per component, conflict-free
-// under the swizzle, and samples TP points at a time with all their corner
-// loads issued before the first lerp.  Corners are addressed from one base
-// pointer per point (CornerStep).  The output is stored directly: the lanes
-// of a warp write 32 consecutive z.  On 8 x 128^3 volumes this takes 0.095 ms
-// against 0.125 ms for k_interpolate_tiled<3, 1>: 110 instead of 183
-// instructions per point, identical results.  Four blocks per SM keep most
-// of L1 for the gathers (77 % sector hits; at six or eight blocks the shared
-// memory carve-out leaves too little L1 and the kernel slows down).
-constexpr int kTmaBox = 3 * kTile * kTile;   // floats per staged grid tile
-constexpr int kTmaSmem = 1024 + 2 * kTmaBox * 4 + 2 * 8;
+// 2D / 3D forward with the grid tile staged by the tensor memory accelerator.
+// One cp.async.bulk.tensor per image copies the tile's box of the grid (2D:
+// 32 x, 32 y, 2 components; 3D: 32 x, 1 y, 32 z, 3 components) into shared
+// memory with the 128-byte swizzle (the 128-byte row of x values of row
+// R = 32 j + z_local has its 16-byte chunks permuted by chunk ^ (R & 7)),
+// double-buffered on two mbarriers, so the staging costs no per-point
+// instructions; points outside the image read the zero fill.  Lane z_local
+// then reads the four x values of its chunk (x_local = 4 warp + u) with one
+// 16-byte load per component, conflict-free under the swizzle, and samples TP
+// points at a time with all their corner loads issued before the first lerp.
+// Corners are addressed from one base pointer per point (CornerStep).  The
+// output is stored directly: the lanes of a warp write 32 consecutive z.
+// Identical results to k_interpolate_tiled, fewer instructions: on 8 x 128^3
+// volumes 0.095 against 0.125 ms (110 instead of 183 instructions per point);
+// on 3 x 224^2 images 0.032 against 0.037 ms at 64 images, 0.311 against
+// 0.323 ms at 1024.  Blocks per SM are capped so that the shared-memory
+// carve-out leaves most of L1 to the gathers (3D at 4 blocks: 77 % sector
+// hits; at 6 or 8 the hit rate and the speed drop).
+template <int N>
+__host__ __device__ constexpr int tma_box() { return N * kTile * kTile; }   // floats per grid tile
+template <int N>
+__host__ __device__ constexpr int tma_smem() { return 1024 + 2 * tma_box<N>() * 4 + 2 * 8; }
 
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1,
+                                            int c2, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
 __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1,
                                             int c2, int c3, uint64_t *bar) {
     asm volatile(
@@ -265,26 +277,38 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
-// Points whose corner loads are issued together, and blocks per SM: the
+// The grid tile of image b into buf (completion on bar).
+template <int N>
+__device__ __forceinline__ void tma_grid_tile(float *buf, const CUtensorMap *map, int a0, int mid,
+                                              int z0, int b, uint64_t *bar) {
+    mbar_arrive_expect_tx(bar, tma_box<N>() * 4);
+    if constexpr (N == 2) tma_load_3d(buf, map, a0, z0, 2 * b, bar);
+    else tma_load_4d(buf, map, a0, mid, z0, 3 * b, bar);
+}
+
+// Points whose corner loads are issued together, and blocks per SM.  3D: the
 // gathered values of one group stay within 64 registers per thread for one
 // or two channels; three channels take one point at a time and up to 80
-// registers (four would spill: they use k_interpolate_tiled<3, 4>).
-template <int CC>
-__host__ __device__ constexpr int tma3_points_per_group() { return CC == 1 ? 4 : 1; }
-template <int CC>
-__host__ __device__ constexpr int tma3_blocks_per_sm() { return CC <= 2 ? 4 : 3; }
+// registers (four would spill: they use k_interpolate_tiled<3, 4>).  2D: one
+// point at a time, 6 blocks per SM (40 registers), 5 for four channels.
+template <int N, int CC>
+__host__ __device__ constexpr int tma_points_per_group() { return N == 3 && CC == 1 ? 4 : 1; }
+template <int N, int CC>
+__host__ __device__ constexpr int tma_blocks_per_sm() {
+    return N == 2 ? (CC <= 3 ? 6 : 5) : CC <= 2 ? 4 : 3;
+}
 
-template <int CC, bool FB>
-__global__ void __launch_bounds__(256, tma3_blocks_per_sm<CC>())
-    k_interpolate_tma3(const __grid_constant__ CUtensorMap gmap, Geo g, TileGeo tg,
-                       const float *__restrict__ data, float *__restrict__ out, int nb,
-                       unsigned *err) {
-    constexpr int N = 3, TP = tma3_points_per_group<CC>();
+template <int N, int CC, bool FB>
+__global__ void __launch_bounds__(256, tma_blocks_per_sm<N, CC>())
+    k_interpolate_tma(const __grid_constant__ CUtensorMap gmap, Geo g, TileGeo tg,
+                      const float *__restrict__ data, float *__restrict__ out, int nb,
+                      unsigned *err) {
+    constexpr int TP = tma_points_per_group<N, CC>(), BOX = tma_box<N>();
     extern __shared__ unsigned char smem_raw[];
     // the swizzle pattern follows address bits 7-9: 1024-byte aligned buffers
     float *gbuf = reinterpret_cast<float *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *bar = reinterpret_cast<uint64_t *>(gbuf + 2 * kTmaBox);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(gbuf + 2 * BOX);
     int a0, z0, mid;
     tile_coords<N>(g, tg, blockIdx.x, a0, z0, mid);
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -296,10 +320,7 @@ __global__ void __launch_bounds__(256, tma3_blocks_per_sm<CC>())
     }
     __syncthreads();
     int b = blockIdx.y;
-    if (leader && b < nb) {
-        mbar_arrive_expect_tx(&bar[0], kTmaBox * 4);
-        tma_load_4d(gbuf, &gmap, a0, mid, z0, 3 * b, &bar[0]);
-    }
+    if (leader && b < nb) tma_grid_tile<N>(gbuf, &gmap, a0, mid, z0, b, &bar[0]);
     const int chunk = ((ty ^ (tx & 7)) << 4);   // byte offset of this lane's x chunk in its row
     for (int k = 0; b < nb; b += gridDim.y, ++k) {
         const int hb = k & 1;
@@ -311,12 +332,10 @@ __global__ void __launch_bounds__(256, tma3_blocks_per_sm<CC>())
             mbar_wait_bounded(&bar[hb], parity);   // a second bounded wait for the copy in flight
             break;
         }
-        if (leader && b + (int)gridDim.y < nb) {
-            mbar_arrive_expect_tx(&bar[hb ^ 1], kTmaBox * 4);
-            tma_load_4d(gbuf + (hb ^ 1) * kTmaBox, &gmap, a0, mid, z0, 3 * (b + gridDim.y),
-                        &bar[hb ^ 1]);
-        }
-        const unsigned char *gt = reinterpret_cast<const unsigned char *>(gbuf + hb * kTmaBox);
+        if (leader && b + (int)gridDim.y < nb)
+            tma_grid_tile<N>(gbuf + (hb ^ 1) * BOX, &gmap, a0, mid, z0, b + gridDim.y,
+                             &bar[hb ^ 1]);
+        const unsigned char *gt = reinterpret_cast<const unsigned char *>(gbuf + hb * BOX);
         float pp[4][N];
 #pragma unroll
         for (int j = 0; j < N; ++j) {
@@ -439,32 +458,42 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
-// The grid [nb, 3, D_out, H_out, W_out] (x fastest) as a 4D tensor map with
-// the (32, 1, 32, 3) box of k_interpolate_tma3.  False where the tensor
-// memory accelerator cannot address it: a grid not 16-byte aligned or a row
-// stride (W_out floats) not a multiple of 16 bytes.
-static bool encode_grid_map_3d(CUtensorMap *map, const float *grid, const int *outsize, int nb) {
+// The grid [nb, N, (D_out,) H_out, W_out] (x fastest) as an (N + 1)-D tensor
+// map with the box of k_interpolate_tma.  False where the tensor memory
+// accelerator cannot address it: a grid not 16-byte aligned or a row stride
+// (W_out floats) not a multiple of 16 bytes.
+static bool encode_grid_map(CUtensorMap *map, int ndim, const float *grid, const int *outsize,
+                            int nb) {
     const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc || (reinterpret_cast<uintptr_t>(grid) & 15u) || (outsize[0] & 3)) return false;
-    const cuuint64_t W = outsize[0], H = outsize[1], D = outsize[2];
-    const cuuint64_t dims[4] = {W, H, D, (cuuint64_t)3 * nb};
-    const cuuint64_t strides[3] = {W * 4, W * H * 4, W * H * D * 4};
-    const cuuint32_t box[4] = {(cuuint32_t)kTile, 1, (cuuint32_t)kTile, 3};
+    cuuint64_t dims[4], strides[3];
+    cuuint32_t box[4];
     const cuuint32_t estr[4] = {1, 1, 1, 1};
-    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float *>(grid), dims, strides,
-               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+    cuuint64_t stride = 4;
+    for (int j = 0; j < ndim; ++j) {
+        dims[j] = (cuuint64_t)outsize[j];
+        stride *= dims[j];
+        strides[j] = stride;   // bytes from one index of axis j + 1 to the next
+        box[j] = (ndim == 3 && j == 1) ? 1u : (cuuint32_t)kTile;
+    }
+    dims[ndim] = (cuuint64_t)ndim * nb;   // (image, component) planes
+    box[ndim] = (cuuint32_t)ndim;
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, ndim + 1, const_cast<float *>(grid), dims,
+               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int CC>
-static cudaError_t launch_tma3(const CUtensorMap &map, const Geo &g, const TileGeo &tg,
-                               dim3 tgrid, const float *data, float *out, int nb, unsigned *err,
-                               cudaStream_t s) {
+template <int N, int CC>
+static cudaError_t launch_tma(const CUtensorMap &map, const Geo &g, const TileGeo &tg,
+                              dim3 tgrid, const float *data, float *out, int nb, unsigned *err,
+                              cudaStream_t s) {
     if (g.nD < (1 << 23))
-        k_interpolate_tma3<CC, true><<<tgrid, 256, kTmaSmem, s>>>(map, g, tg, data, out, nb, err);
+        k_interpolate_tma<N, CC, true>
+            <<<tgrid, 256, tma_smem<N>(), s>>>(map, g, tg, data, out, nb, err);
     else
-        k_interpolate_tma3<CC, false><<<tgrid, 256, kTmaSmem, s>>>(map, g, tg, data, out, nb, err);
+        k_interpolate_tma<N, CC, false>
+            <<<tgrid, 256, tma_smem<N>(), s>>>(map, g, tg, data, out, nb, err);
     return cudaGetLastError();
 }
 
@@ -485,11 +514,19 @@ cudaError_t launch_interpolate(int ndim, const float *data, int nb, int C, const
     const int ipb = ndim == 3 ? images_per_block<3>() : images_per_block<2>();
     const dim3 tgrid(blocks, (gridn.y + ipb - 1) / ipb);
     CUtensorMap map;
-    if (ndim == 3 && C <= 3 && encode_grid_map_3d(&map, grid, outsize, nb)) {
+    if (C <= (ndim == 3 ? 3 : 4) && encode_grid_map(&map, ndim, grid, outsize, nb)) {
+        if (ndim == 2) {
+            switch (C) {
+                case 1: return launch_tma<2, 1>(map, g, tg, tgrid, data, out, nb, err, s);
+                case 2: return launch_tma<2, 2>(map, g, tg, tgrid, data, out, nb, err, s);
+                case 3: return launch_tma<2, 3>(map, g, tg, tgrid, data, out, nb, err, s);
+                default: return launch_tma<2, 4>(map, g, tg, tgrid, data, out, nb, err, s);
+            }
+        }
         switch (C) {
-            case 1: return launch_tma3<1>(map, g, tg, tgrid, data, out, nb, err, s);
-            case 2: return launch_tma3<2>(map, g, tg, tgrid, data, out, nb, err, s);
-            default: return launch_tma3<3>(map, g, tg, tgrid, data, out, nb, err, s);
+            case 1: return launch_tma<3, 1>(map, g, tg, tgrid, data, out, nb, err, s);
+            case 2: return launch_tma<3, 2>(map, g, tg, tgrid, data, out, nb, err, s);
+            default: return launch_tma<3, 3>(map, g, tg, tgrid, data, out, nb, err, s);
         }
     }
 #define CPAB_IT(NN, CC) k_interpolate_tiled<NN, CC><<<tgrid, block, 0, s>>>(g, tg, data, C, grid, out, nb)
