@@ -328,9 +328,10 @@ CPAB_API int cpab_findcellidx(int ndim, const int *nc, const float *points, long
  * CPAB_DEV_BAD_OFFSETS).  total = number of value elements; total + 128*S
  * must be below 2^31.  A and E are [S, nC, 1, 2] (one theta per series, from
  * cpab_cell_tables); basis is [2*nC, d]; dtheta is [S, d].  workspace is
- * device memory of cpab_ragged1d_workspace() bytes (warp-tile prefix and the
- * deterministic partial sums); the calls do not synchronise and can be
- * captured in a CUDA graph.
+ * device memory of cpab_ragged1d_workspace() bytes (warp-tile prefix, the
+ * deterministic partial sums and, for nc <= 128, the adjoint's per-lane cell
+ * sums: 256 * nc bytes per resident warp, 32 warps per SM); the calls do not
+ * synchronise and can be captured in a CUDA graph.
  */
 CPAB_API size_t cpab_ragged1d_workspace(int nc, int nsteps, int S);
 

@@ -433,16 +433,31 @@ __device__ __forceinline__ void warp_flush_1d(bool flush, int cell, const float 
     __syncwarp();
 }
 
+// Where reverse_sweep puts a lane's accumulated dL/dA of a cell when the lane
+// leaves it: the warp's cell table, through warp_flush / warp_flush_1d
+// (called by all lanes of the warp).
+template <int N>
+struct WarpTabSink {
+    float *warp_tab;
+    template <int P>
+    __device__ __forceinline__ void operator()(bool flush, int cell,
+                                               const float (&acc)[P]) const {
+        if constexpr (N == 1) warp_flush_1d<P>(flush, cell, acc, warp_tab);
+        else warp_flush<P>(flush, cell, acc, warp_tab);
+    }
+};
+
 // Reverse sweep of one trajectory whose cells are logged in cl and whose
 // checkpoints are in ck; lam holds dL/dp_N on entry and dL/dp_0 on exit.
 // Each segment's positions are rebuilt from its checkpoint with the logged
 // cells (no lookups) into pb, then walked backwards.  The loops are not
 // unrolled: the body stays small enough for the instruction cache.
-// Executed by all lanes of the warp (uniform trip counts).
-template <int N, int MODE, typename CT>
-__device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nsteps,
-                                              const Steps &st, bool live, float (&lam)[N],
-                                              float *warp_tab) {
+// Executed by all lanes of the warp (uniform trip counts); sink(flush, cell,
+// acc) receives each lane's sum over a run of steps in one cell.
+template <int N, int MODE, typename CT, typename Sink>
+__device__ __forceinline__ void reverse_sweep_to(const AdjSmem<N, CT> &sm, int nsteps,
+                                                 const Steps &st, bool live, float (&lam)[N],
+                                                 Sink &sink) {
     constexpr int P = N * (N + 1);
     const int B = blockDim.x, tid = threadIdx.x;
     const int nseg = (nsteps + kSeg - 1) / kSeg;
@@ -467,8 +482,7 @@ __device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nste
         for (int s = len - 1; s >= 0; --s) {
             const int c = (int)sm.cl[(n0 + s) * B + tid];
             const bool change = c != gcell;
-            if constexpr (N == 1) warp_flush_1d<P>(change && gcell >= 0 && live, gcell, acc, warp_tab);
-            else warp_flush<P>(change && gcell >= 0 && live, gcell, acc, warp_tab);
+            sink(change && gcell >= 0 && live, gcell, acc);
             if (change) {
                 gcell = c;
 #pragma unroll
@@ -480,8 +494,15 @@ __device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nste
             adjoint_step<N>(sm.dtab, c, p, lam, acc);
         }
     }
-    if constexpr (N == 1) warp_flush_1d<P>(gcell >= 0 && live, gcell, acc, warp_tab);
-    else warp_flush<P>(gcell >= 0 && live, gcell, acc, warp_tab);
+    sink(gcell >= 0 && live, gcell, acc);
+}
+
+template <int N, int MODE, typename CT>
+__device__ __forceinline__ void reverse_sweep(const AdjSmem<N, CT> &sm, int nsteps,
+                                              const Steps &st, bool live, float (&lam)[N],
+                                              float *warp_tab) {
+    WarpTabSink<N> sink{warp_tab};
+    reverse_sweep_to<N, MODE, CT>(sm, nsteps, st, live, lam, sink);
 }
 
 // Sweep with the arithmetic of k_integrate's compensated path,

@@ -196,6 +196,8 @@ struct RaggedBwd {
     float *dvalues;        // [total] (optional, accumulated)
     float *partials;       // [(TW + S)][nC * 2]  (set from the workspace)
     float *sse_partials;   // [(TW + S)]          (set from the workspace)
+    float *lane_slots;     // [TW][nC][2][32] per-lane cell sums, nC <= kLaneSlotCells
+                           // (set from the workspace)
 };
 // fused = true: dL/d(out) from the MSE residual against `target`, per-series
 // sum of squared residuals into sse[S]; fused = false: dL/d(out) = gout.

@@ -186,7 +186,31 @@ __host__ __device__ inline size_t ragged_adjoint_smem(int nC, int nsteps, int bl
     return (b + 15) & ~(size_t)15;
 }
 
-template <int MODE, typename CT, bool FUSED>
+// The lane-slot sink of the reverse sweep (LS = true): a lane that leaves a
+// cell adds its sum over the steps spent there into its own slots
+// ls[cell][i][lane] with fire-and-forget global reductions, and widens the
+// range [lo, hi] of cells it touched.  Each slot is written by one lane only,
+// in program order, so its value does not depend on timing; the warp sums the
+// 32 slots of each touched cell with a fixed shuffle tree when it finishes a
+// series (reproducible dtheta).  Unlike the warp-table flush (a five-round
+// shuffle tree over the run of lanes in a cell, executed by the whole warp at
+// every step where any lane changes cell), a lane's flush is two reductions.
+struct LaneSlotSink {
+    float *ls;
+    int lo, hi;
+    template <int P>
+    __device__ __forceinline__ void operator()(bool flush, int cell, const float (&acc)[P]) {
+        if (flush) {
+            float *q = ls + cell * (P * 32) + (threadIdx.x & 31);
+#pragma unroll
+            for (int i = 0; i < P; ++i) atomicAdd(q + i * 32, acc[i]);
+            lo = min(lo, cell);
+            hi = max(hi, cell);
+        }
+    }
+};
+
+template <int MODE, typename CT, bool FUSED, bool LS>
 __global__ void __launch_bounds__(256)
     k_ragged_adjoint(Tess t, int nsteps, Steps st, int S, const long long *__restrict__ off,
                      const int *__restrict__ tile_off, int ppt, RaggedBwd a,
@@ -220,6 +244,11 @@ __global__ void __launch_bounds__(256)
     int s = find_series(tile_off, S, (int)t0);
     int s_end = __ldg(tile_off + s + 1);
     float sse = 0.f;
+    LaneSlotSink slots{LS ? a.lane_slots + (size_t)w * t.nC * (P * 32) : nullptr, INT_MAX, -1};
+    if constexpr (LS) {
+        float4 *z = reinterpret_cast<float4 *>(slots.ls);
+        for (int i = lane; i < t.nC * (P * 8); i += 32) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
 
     auto stage = [&](int sid) {
         __syncwarp();
@@ -234,6 +263,31 @@ __global__ void __launch_bounds__(256)
     };
     auto finish = [&](int sid) {
         __syncwarp();
+        if constexpr (LS) {
+            // cell sums of the series into gw; the slots are zeroed for the next one
+            const int lo = __reduce_min_sync(0xffffffffu, slots.lo);
+            const int hi = __reduce_max_sync(0xffffffffu, slots.hi);
+            for (int c = lo; c <= hi; ++c) {
+                float *q = slots.ls + c * (P * 32) + lane;
+                float v[P];
+#pragma unroll
+                for (int i = 0; i < P; ++i) {
+                    v[i] = __ldcg(q + i * 32);   // this lane's own reductions, in order
+                    q[i * 32] = 0.f;
+                }
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1)
+#pragma unroll
+                    for (int i = 0; i < P; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], d);
+                if (lane == 0) {
+#pragma unroll
+                    for (int i = 0; i < P; ++i) sm.gw[c * P + i] = v[i];
+                }
+            }
+            slots.lo = INT_MAX;
+            slots.hi = -1;
+            __syncwarp();
+        }
         float v = sse;
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
@@ -282,7 +336,8 @@ __global__ void __launch_bounds__(256)
                               gf);
                 lam[0] = gf[0] * g.sizem1[0];
             }
-            reverse_sweep<1, MODE, CT>(sm, nsteps, st, live, lam, sm.gw);
+            if constexpr (LS) reverse_sweep_to<1, MODE, CT>(sm, nsteps, st, live, lam, slots);
+            else reverse_sweep<1, MODE, CT>(sm, nsteps, st, live, lam, sm.gw);
         }
     }
     finish(s);
@@ -296,23 +351,35 @@ std::map<std::tuple<int, int, int, int, int, int, long long>, std::pair<int, int
 
 }  // namespace
 
+// Lane slots (the adjoint's per-lane cell sums, k_ragged_adjoint<..., true>)
+// for tessellations of at most kLaneSlotCells cells, sized for at most
+// kLaneSlotWarpsPerSM resident warps per SM (the kernel's grid is capped to it).
+constexpr int kLaneSlotCells = 128, kLaneSlotWarpsPerSM = 32;
+
+static size_t lane_slot_bytes(const Tess &t) {
+    if (t.nC > kLaneSlotCells) return 0;
+    return (size_t)num_sms() * kLaneSlotWarpsPerSM * t.nC * 2 * 32 * 4;
+}
+
 size_t ragged_workspace_bytes(const Tess &t, int S) {
     const size_t tiles = ((size_t)(S + 1) * 4 + 255) & ~(size_t)255;
     const size_t slots = (size_t)num_sms() * 64 + (size_t)S;
     const size_t part = (slots * t.nC * 2 * 4 + 255) & ~(size_t)255;
     const size_t sse = (slots * 4 + 255) & ~(size_t)255;
-    return tiles + part + sse;
+    return tiles + part + sse + lane_slot_bytes(t);
 }
 
 static void ragged_carve(const Tess &t, int S, void *ws, int **tile_off, float **partials,
-                         float **sse_partials) {
+                         float **sse_partials, float **lane_slots) {
     char *p = static_cast<char *>(ws);
     const size_t tiles = ((size_t)(S + 1) * 4 + 255) & ~(size_t)255;
     const size_t slots = (size_t)num_sms() * 64 + (size_t)S;
     const size_t part = (slots * t.nC * 2 * 4 + 255) & ~(size_t)255;
+    const size_t sse = (slots * 4 + 255) & ~(size_t)255;
     *tile_off = reinterpret_cast<int *>(p);
     *partials = reinterpret_cast<float *>(p + tiles);
     *sse_partials = reinterpret_cast<float *>(p + tiles + part);
+    *lane_slots = lane_slot_bytes(t) ? reinterpret_cast<float *>(p + tiles + part + sse) : nullptr;
 }
 
 bool ragged_get_tuned(int kind, int mode, const Tess &t, int nsteps, int S, long long total,
@@ -361,8 +428,8 @@ cudaError_t launch_ragged_forward(const Tess &t, int nsteps, int block, int ppt,
                                   const float *values, float *out, void *ws,
                                   unsigned long long *ties, unsigned *err, cudaStream_t s) {
     int *tile_off;
-    float *partials, *ssep;
-    ragged_carve(t, S, ws, &tile_off, &partials, &ssep);
+    float *partials, *ssep, *lane_slots;
+    ragged_carve(t, S, ws, &tile_off, &partials, &ssep, &lane_slots);
     if (S == 0) return cudaSuccess;
     k_ragged_plan<<<1, 1024, 0, s>>>(S, off, total, 32 * ppt, tile_off, err);
     cudaError_t e = cudaGetLastError();
@@ -374,12 +441,12 @@ cudaError_t launch_ragged_forward(const Tess &t, int nsteps, int block, int ppt,
     }
 }
 
-template <int MODE, typename CT, bool FUSED>
-static cudaError_t launch_ra_t(const Tess &t, int nsteps, int block, int ppt, int S,
-                               const long long *off, const int *tile_off, const RaggedBwd &a,
-                               const float *basis, int d, float *dtheta, float *sse,
-                               unsigned long long *ties, unsigned *err, cudaStream_t s) {
-    auto kern = k_ragged_adjoint<MODE, CT, FUSED>;
+template <int MODE, typename CT, bool FUSED, bool LS>
+static cudaError_t launch_ra_ls(const Tess &t, int nsteps, int block, int ppt, int S,
+                                const long long *off, const int *tile_off, const RaggedBwd &a,
+                                const float *basis, int d, float *dtheta, float *sse,
+                                unsigned long long *ties, unsigned *err, cudaStream_t s) {
+    auto kern = k_ragged_adjoint<MODE, CT, FUSED, LS>;
     const size_t smem = ragged_adjoint_smem<MODE, CT>(t.nC, nsteps, block);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -387,8 +454,10 @@ static cudaError_t launch_ra_t(const Tess &t, int nsteps, int block, int ppt, in
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
     if (per_sm <= 0) return cudaErrorInvalidConfiguration;
-    // partial slots are sized for at most 64 resident warps per SM
-    const int grid = min(num_sms() * per_sm, num_sms() * 64 / (block / 32));
+    // partial slots are sized for at most 64 resident warps per SM, lane slots
+    // for kLaneSlotWarpsPerSM
+    const int grid = min(num_sms() * per_sm,
+                         num_sms() * (LS ? kLaneSlotWarpsPerSM : 64) / (block / 32));
     const Steps st = make_steps(nsteps);
     kern<<<grid, block, smem, s>>>(t, nsteps, st, S, off, tile_off, ppt, a, ties, err);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -401,6 +470,18 @@ static cudaError_t launch_ra_t(const Tess &t, int nsteps, int block, int ppt, in
     fin<<<S, 256, fsmem, s>>>(t.nC, st, S, tile_off, grid * (block / 32), a.partials,
                               a.sse_partials, a.A, basis, d, dtheta, sse);
     return cudaGetLastError();
+}
+
+template <int MODE, typename CT, bool FUSED>
+static cudaError_t launch_ra_t(const Tess &t, int nsteps, int block, int ppt, int S,
+                               const long long *off, const int *tile_off, const RaggedBwd &a,
+                               const float *basis, int d, float *dtheta, float *sse,
+                               unsigned long long *ties, unsigned *err, cudaStream_t s) {
+    if (a.lane_slots)
+        return launch_ra_ls<MODE, CT, FUSED, true>(t, nsteps, block, ppt, S, off, tile_off, a,
+                                                   basis, d, dtheta, sse, ties, err, s);
+    return launch_ra_ls<MODE, CT, FUSED, false>(t, nsteps, block, ppt, S, off, tile_off, a,
+                                                basis, d, dtheta, sse, ties, err, s);
 }
 
 // Shared-memory bytes of the adjoint kernel for this block size (0 if the
@@ -428,7 +509,7 @@ cudaError_t launch_ragged_adjoint(const Tess &t, int nsteps, int mode, bool fuse
                                   unsigned *err, cudaStream_t s) {
     int *tile_off;
     RaggedBwd a = a_in;
-    ragged_carve(t, S, ws, &tile_off, &a.partials, &a.sse_partials);
+    ragged_carve(t, S, ws, &tile_off, &a.partials, &a.sse_partials, &a.lane_slots);
     if (S == 0) return cudaSuccess;
     k_ragged_plan<<<1, 1024, 0, s>>>(S, off, total, 32 * ppt, tile_off, err);
     cudaError_t e = cudaGetLastError();
