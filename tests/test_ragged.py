@@ -102,11 +102,13 @@ def _dv_close(a, b, absum, L=None):
 LENGTHS = [0, 1, 2, 3, 31, 32, 33, 63, 64, 65, 0, 97, 128, 129, 200, 257, 511, 600, 5, 1000]
 
 
-@pytest.fixture(scope='module')
-def small(cuda):
+# 20 cells: the adjoint sums per lane in workspace slots; 150 cells (above
+# 128): the per-step warp flush into the warp's cell table.
+@pytest.fixture(scope='module', params=[20, 150])
+def small(cuda, request):
     rng = np.random.default_rng(7)
     lengths = LENGTHS + [int(x) for x in rng.integers(1, 400, size=20)]
-    return _problem(cuda, 20, lengths)
+    return _problem(cuda, request.param, lengths)
 
 
 def test_ragged_forward_matches_per_series_path(small, oracle):
