@@ -441,8 +441,8 @@ static TileGeo make_tiles(int ndim, const Geo &g, unsigned *blocks) {
     return tg;
 }
 
-// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
-// against the driver library); null where the driver does not provide it.
+// cuTensorMapEncodeTiled through the CUDA runtime's entry-point query (no link
+// against libcuda); null where the installed CUDA driver does not provide it.
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void *f = nullptr;
